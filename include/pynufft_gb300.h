@@ -1,0 +1,150 @@
+/*
+ * pynufft_gb300 — C ABI of the GB300 (sm_103a) min-max NUFFT.
+ *
+ * This is the drop-in boundary for the reference class `NUFFT`
+ * (pynufft 2025.2.1, nufft/__init__.py:496-738).  Every entry point takes
+ * plain pointers and sizes, returns an `int` status (NUFFT_OK == 0) and runs
+ * asynchronously on the caller's CUDA stream (`stream` is a cudaStream_t
+ * passed as void*; NULL means the legacy default stream).
+ *
+ * Array conventions (all complex data is interleaved float32 pairs,
+ * i.e. numpy complex64 / C float _Complex):
+ *   om : M x ndim float64, C order, normalised frequencies in radians
+ *        (any range; wrapped modulo the oversampled grid).
+ *   x  : Nd + (batch,) image, C order, batch (coil) fastest.
+ *   k  : Kd + (batch,) oversampled k-space grid, C order, batch fastest.
+ *   y  : (M, batch) non-uniform samples, batch fastest.
+ *   With ninst > 1 independent instances, x, k and y gain a leading instance
+ *   axis for x and k ((ninst,) + Nd + (batch,)) and y is the concatenation of
+ *   the instances' samples in instance order.
+ * Device pointers must be 16-byte aligned (true of every cudaMalloc/torch
+ * allocation).  The plan owns its tables and workspace; inputs are never
+ * written; outputs are fully overwritten.  Calls on one plan must be
+ * serialised (one stream at a time); distinct plans are independent.
+ */
+#ifndef PYNUFFT_GB300_H
+#define PYNUFFT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the Python layer maps them to the reference's exception
+ *      types: TypeError/KeyError for plan arguments, ValueError, RuntimeError) */
+#define NUFFT_OK                 0
+#define NUFFT_EINVAL             1  /* bad argument, shape or size            */
+#define NUFFT_EOM_NONFINITE      2  /* om holds NaN or Inf                    */
+#define NUFFT_ENOMEM             3  /* device allocation failed               */
+#define NUFFT_ECUDA              4  /* CUDA runtime error                     */
+#define NUFFT_ECUFFT             5  /* cuFFT error                            */
+#define NUFFT_ENOPOINTS          6  /* nufft_set_points has not been called   */
+#define NUFFT_ECG_BREAKDOWN      7  /* CG: p^H A p <= 0 or not finite         */
+#define NUFFT_EUNSUPPORTED       8  /* valid request this build does not do   */
+
+/* ---- plan flags */
+#define NUFFT_FLAG_DETERMINISTIC 1  /* bitwise-reproducible gridding (y2k)    */
+
+typedef struct nufft_plan_s* nufft_plan_t;
+
+/* Human-readable text of the last error raised on the calling thread. */
+const char* nufft_last_error(void);
+
+/* Library version string, e.g. "pynufft_gb300 0.1.0 (sm_103a)". */
+const char* nufft_version(void);
+
+/* Plan-time numerics of one axis, host only (no GPU needed).  Replaces
+ * helper.nufft_alpha_kb_fit / nufft_scale1 / nufft_T
+ * (src/_helper/helper.py:910-958, 1015-1036, 1060-1083).
+ *   alpha_in  : NULL to fit the cosine-series coefficients here, or the L_in+1
+ *               coefficients to use (e.g. the reference's own float32 fit)
+ *   alpha_out : float[16]  coefficients used (L+1 valid, L <= 14)
+ *   L_out     : series order L
+ *   sn_out    : double[N]  real scaling factor of this axis
+ *   T_out     : double[J*J] pinv(CSSC), row major                     */
+int nufft_axis_params(int N, int J, int K, const float* alpha_in, int L_in,
+                      float* alpha_out, int* L_out, double* sn_out, double* T_out);
+
+/* Create a plan.  Replaces NUFFT.plan(om, Nd, Kd, Jd[, batch])
+ * (nufft/__init__.py:552-596 -> _plan_cpu, nufft/_nufft_class_methods_cpu.py:27-124;
+ *  batch semantics of linalg/nufft_hsa.py:152-242).  ndim in 1..3,
+ * Jd[d] <= 16, Jd[d] <= Kd[d], Nd[d] <= Kd[d]; batch >= 1; ninst >= 1.
+ * Allocates the plan's device workspace on the current device. */
+int nufft_plan_create(int ndim, const int* Nd, const int* Kd, const int* Jd,
+                      int batch, int ninst, int flags, nufft_plan_t* plan_out);
+
+/* Replace the cosine-series coefficients of one axis (L+1 values, L <= 14)
+ * and re-derive its scaling factor and interpolator normal matrix.  Call
+ * before nufft_set_points.  The reference fits these coefficients with a
+ * complex64 least-squares solve (helper.py:949-958); a caller that has that
+ * fit reproduces the reference's interpolator exactly. */
+int nufft_plan_set_alpha(nufft_plan_t plan, int axis, const float* alpha, int L);
+
+/* Set the non-uniform points: counts[i] points of instance i, om holding
+ * sum(counts) rows of ndim float64 (instances concatenated).  om may be a
+ * host or a device pointer (om_on_device).  Builds the bin-sorted per-axis
+ * interpolation tables on the device (the GPU counterpart of the CSR build in
+ * helper.plan, src/_helper/helper.py:736-786).  Synchronises `stream` once. */
+int nufft_set_points(nufft_plan_t plan, const int64_t* counts, const double* om,
+                     int om_on_device, void* stream);
+
+int nufft_plan_destroy(nufft_plan_t plan);
+
+/* Per-plan tuning: bin shape (cells per axis) and the largest number of
+ * points one thread block takes from a bin.  Takes effect at the next
+ * nufft_set_points.  Zero entries keep the default. */
+int nufft_plan_set_bins(nufft_plan_t plan, const int* bin_shape, int max_sub_points);
+
+/* Query plan geometry: total points, number of gridding sub-problems and
+ * bytes of device memory the plan holds. */
+int nufft_plan_info(nufft_plan_t plan, int64_t* M_total, int64_t* n_subproblems,
+                    int64_t* device_bytes);
+
+/* ---- the six stages (nufft/__init__.py:658-692) ---------------------------
+ * x2xx  (_x2xx_cpu  :224-230)  xx = x * sn                       Nd -> Nd
+ * xx2k  (_xx2k_cpu  :232-249)  k  = fftn(zero-pad(xx))           Nd -> Kd
+ * k2y   (_k2y_cpu   :273-288)  y  = interpolate(k)               Kd -> M
+ * y2k   (_y2k_cpu   :290-314)  k  = grid(y) (adjoint of k2y)     M  -> Kd
+ * k2xx  (_k2xx_cpu  :316-329)  xx = crop(ifftn(k)), 1/prod(Kd)   Kd -> Nd
+ * xx2x  (_xx2x_cpu  :346-351)  x  = xx * sn                      Nd -> Nd */
+int nufft_x2xx(nufft_plan_t plan, const void* x, void* xx, void* stream);
+int nufft_xx2k(nufft_plan_t plan, const void* xx, void* k, void* stream);
+int nufft_k2y(nufft_plan_t plan, const void* k, void* y, void* stream);
+int nufft_y2k(nufft_plan_t plan, const void* y, void* k, void* stream);
+int nufft_k2xx(nufft_plan_t plan, const void* k, void* xx, void* stream);
+int nufft_xx2x(nufft_plan_t plan, const void* xx, void* x, void* stream);
+
+/* forward (_forward_cpu :168-179): y = k2y(xx2k(x2xx(x))), sn-scale and
+ * zero-pad fused into one pass ahead of the FFT. */
+int nufft_forward(nufft_plan_t plan, const void* x, void* y, void* stream);
+/* adjoint (_adjoint_cpu :181-193): x = xx2x(k2xx(y2k(y))), crop, 1/prod(Kd)
+ * and sn-scale fused into one pass after the inverse FFT. */
+int nufft_adjoint(nufft_plan_t plan, const void* y, void* x, void* stream);
+/* selfadjoint (_selfadjoint_cpu :201-214) = adjoint(forward(x)). */
+int nufft_selfadjoint(nufft_plan_t plan, const void* x, void* x_out, void* stream);
+/* k2y2k (_k2y2k_cpu :353-362) = y2k(k2y(k)). */
+int nufft_k2y2k(nufft_plan_t plan, const void* k, void* k_out, void* stream);
+
+/* solve(y, 'cg', maxiter) (linalg/solve_cpu.py:256-288): conjugate gradients
+ * on the k-space normal operator y2k.k2y with x0 = 0 and scipy's stopping
+ * rule ||r|| < max(atol, rtol*||b||), then x = k2xx(k) / sn.  maxiter < 0
+ * means scipy's default of 10 * prod(Kd).  The set-up and chunks of
+ * up to 32 iterations run as captured CUDA graphs with device-side scalars
+ * (FP64 dots and norms); a solve longer than one chunk checks convergence on
+ * the host between chunks.  Each coil/instance is an independent system.
+ * iters_out (host pointer, may be NULL) receives the most iterations any
+ * system ran; reading it synchronises `stream`. */
+int nufft_solve_cg(nufft_plan_t plan, const void* y, void* x, int maxiter,
+                   double rtol, double atol, int* iters_out, void* stream);
+
+/* Trajectory gradient support: dy[m, d] = sum_n x_n (-i (n_d - N_d/2))
+ * e^{-i om_m.(n - N/2)}, evaluated with the plan's interpolator as the
+ * forward transform of (-i (n_d - N_d/2)) x.  dy is ndim consecutive (M,batch)
+ * blocks. */
+int nufft_forward_dom(nufft_plan_t plan, const void* x, void* dy, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYNUFFT_GB300_H */

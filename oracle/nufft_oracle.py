@@ -1,0 +1,414 @@
+"""Oracle: a CPU restatement of PyNUFFT's numpy min-max NUFFT path.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker for the CUDA path: the
+parity tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU legs import
+it; the product package never does.
+
+It restates, in numpy/scipy, the algorithm of the reference package
+(pynufft 2025.2.1); every function names the reference lines it follows:
+
+* plan numerics                 src/_helper/helper.py:620-802
+* Kaiser-Bessel fit / scaling   src/_helper/helper.py:910-1050
+* min-max interpolator          src/_helper/helper.py:606-618, 1060-1117, 148-210
+* CSR interpolation matrix      src/_helper/helper.py:285-311, 449-480
+* the six stages + solve('cg')  nufft/_nufft_class_methods_cpu.py:27-362,
+                                linalg/solve_cpu.py:256-288
+* exact NUDFT                   linalg/nudft_cpu.py:27-41, 92-103
+
+Dtypes follow the reference on numpy >= 2: the scaling factor is stored as
+complex64, the oversampled FFT runs in complex64, the CSR holds complex128, so
+``k2y``/``y2k`` return complex128 and ``k2xx`` runs its inverse FFT at the
+precision of its input before cropping into complex64.
+
+The oracle is pinned against outputs of the reference itself
+(``tests/golden/make_golden.py`` imports the reference, writes the fixtures,
+and ``tests/test_oracle_golden.py`` checks this module against them) and
+against the exact-NDFT known-answer vectors shipped with the reference
+(``tests/tmp2d_{1,2,3}_.mat``, converted to ``tests/golden/ndft_known_answer.npz``).
+"""
+from __future__ import annotations
+
+import math
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+import scipy.linalg
+import scipy.sparse
+import scipy.special
+
+# Kaiser-Bessel "best" alpha/J ratios for K/N == 2 (src/_helper/helper.py:972-987).
+_KB_BEST_RATIO = {2: 2.5, 3: 2.27, 4: 2.31, 5: 2.34, 6: 2.32, 7: 2.32, 8: 2.35,
+                  9: 2.34, 10: 2.34, 11: 2.35, 12: 2.34, 13: 2.35, 14: 2.35,
+                  15: 2.35, 16: 2.33}
+
+
+# --------------------------------------------------------------------------
+# plan-time numerics
+# --------------------------------------------------------------------------
+def kb_shape(J: int, K_over_N: float) -> float:
+    """Kaiser-Bessel shape parameter (src/_helper/helper.py:961-997)."""
+    if K_over_N != 2:
+        return 2.34 * J
+    if J in _KB_BEST_RATIO:
+        return J * _KB_BEST_RATIO[J]
+    keys = np.array(sorted(_KB_BEST_RATIO))
+    return J * _KB_BEST_RATIO[int(keys[np.argmin(np.abs(keys - J))])]
+
+
+def kb_ft(u, J: int, alpha: float):
+    """Fourier transform of the KB window, order m=0, d=1
+    (src/_helper/helper.py:1000-1012)."""
+    u = np.asarray(u) * (1.0 + 0.0j)
+    z = np.sqrt((2 * np.pi * (J / 2) * u) ** 2.0 - alpha ** 2.0)
+    nu = 0.5
+    y = ((2 * np.pi) ** 0.5) * (J / 2) / scipy.special.iv(0, alpha) \
+        * scipy.special.jv(nu, z) / (z ** nu)
+    return np.real(y)
+
+
+def alpha_beta_fit(N: int, J: int, K: int):
+    """Cosine-series fit of 1/KB_ft (src/_helper/helper.py:910-958).
+
+    Returns ``(alpha, beta)``; ``alpha`` is float32 of length L+1 because the
+    reference solves the least-squares problem in complex64.
+    """
+    beta = 1
+    Nmid = (N - 1.0) / 2.0
+    L = 13 if N > 40 else int(np.ceil(N / 3))
+    nlist = np.arange(N) * 1.0 - Nmid
+    if J > 1:
+        sn_kaiser = 1.0 / kb_ft(nlist / K, J, kb_shape(J, K / N))
+    else:
+        sn_kaiser = np.ones(N)
+    gam = 2 * np.pi / K
+    X = np.cos(np.outer(beta * gam * nlist, np.arange(L + 1)))
+    X = np.asarray(X, dtype=np.complex64)
+    rhs = np.asarray(np.conj(sn_kaiser).reshape(N, 1), dtype=np.complex64)
+    coef = np.linalg.lstsq(np.nan_to_num(X), np.nan_to_num(rhs), rcond=-1)[0]
+    alpha = coef[:, 0].copy()
+    if J > 1:
+        alpha[1:] = alpha[1:] / 2.0
+    else:
+        alpha[0] = 1.0
+        alpha[1:] = 0.0
+    return np.real(alpha).astype(np.float32), beta
+
+
+def scale_axis(N: int, K: int, alpha, beta) -> np.ndarray:
+    """Per-axis image-domain scaling factor, real part
+    (src/_helper/helper.py:1015-1036, 558-584, 780)."""
+    alpha = np.asarray(alpha)
+    L = alpha.size - 1
+    n = np.arange(N, dtype=np.float64)
+    Nmid = (N - 1) / 2.0
+    sn = np.zeros(N, dtype=np.complex128)
+    ph = 1j * (2 * np.pi / K) * (n - Nmid) * beta
+    for l1 in range(-L, L + 1):
+        sn = sn + alpha[abs(l1)].astype(np.float64) * np.exp(ph * l1)
+    return sn.real
+
+
+def minmax_T(N: int, J: int, K: int, alpha, beta) -> np.ndarray:
+    """T = pinv(CSSC), the J x J min-max normal matrix
+    (src/_helper/helper.py:1060-1083).  alpha products are formed in float32
+    first, as the reference does with its float32 coefficient array."""
+    alpha = np.asarray(alpha, dtype=np.float32)
+    L = alpha.size - 1
+    j1, j2 = np.mgrid[1:J + 1, 1:J + 1]
+    overlap = (j2 - j1).astype(np.float64)
+    cssc = np.zeros((J, J))
+    for l1 in range(-L, L + 1):
+        for l2 in range(-L, L + 1):
+            a12 = np.float32(alpha[abs(l1)] * alpha[abs(l2)])
+            cssc = cssc + np.float64(a12) * np.sinc((overlap + beta * (l1 - l2)) / (K / N))
+    return scipy.linalg.pinv(cssc)
+
+
+def minmax_axis(om_d, N: int, J: int, K: int, alpha, beta, T=None):
+    """Per-axis interpolation coefficients and grid indices.
+
+    Follows min_max/nufft_r/OMEGA_u/OMEGA_k/nufft_offset
+    (src/_helper/helper.py:606-618, 1086-1117, 148-210, 900-907).
+    Returns ``ud`` (M x J complex128, already conjugated as in the reference's
+    CSR) and ``kd`` (M x J int64 grid indices along this axis, mod K).
+    """
+    om_d = np.asarray(om_d, dtype=np.float64).ravel()
+    if T is None:
+        T = minmax_T(N, J, K, alpha, beta)
+    alpha = np.asarray(alpha, dtype=np.float32)
+    L = alpha.size - 1
+    gam = 2.0 * np.pi / K
+    koff = np.floor(om_d / gam - J / 2.0)
+    dk = om_d / gam - koff
+    arg = np.add.outer(-np.arange(1, J + 1) * 1.0, dk)            # J x M
+    r = np.zeros(arg.shape)
+    for l1 in range(-L, L + 1):
+        r = r + np.float64(alpha[abs(l1)]) * np.sinc((arg + l1 * beta) / (K / N))
+    c = T.dot(r)
+    u = np.exp(1j * gam * (N - 1.0) / 2.0 * arg) * c * np.exp(-1j * om_d * N / 2.0)
+    ud = u.T.conj()
+    kd = np.mod(np.add.outer(np.arange(1, J + 1), koff.astype(np.int64)), K).T
+    return ud, kd
+
+
+def interp_csr(om, Nd, Kd, Jd, params=None):
+    """The M x prod(Kd) complex128 interpolation matrix
+    (src/_helper/helper.py:449-480 Khatri-Rao, 285-311 create_csr).
+    Row m, entry (j_0..j_{d-1}) with the last axis fastest."""
+    om = np.asarray(om, dtype=np.float64)
+    M, d = om.shape
+    if params is None:
+        params = [alpha_beta_fit(Nd[i], Jd[i], Kd[i]) for i in range(d)]
+    uu = None
+    kk = None
+    for i in range(d):
+        a, b = params[i]
+        ud, kd = minmax_axis(om[:, i], Nd[i], Jd[i], Kd[i], a, b)
+        stride = int(np.prod(Kd[i + 1:])) if i < d - 1 else 1
+        kd = kd * stride
+        if uu is None:
+            uu, kk = ud, kd
+        else:
+            uu = np.einsum('mi,mj->mij', uu, ud).reshape(M, -1)
+            kk = (kk[:, :, None] + kd[:, None, :]).reshape(M, -1)
+    P = int(np.prod(Jd))
+    indptr = np.arange(0, (M + 1) * P, P, dtype=np.int64)
+    return scipy.sparse.csr_matrix((uu.ravel(), kk.ravel(), indptr),
+                                   shape=(M, int(np.prod(Kd))))
+
+
+def check_plan_args(Nd, Kd, Jd):
+    """Argument checks of helper.plan (src/_helper/helper.py:644-654)."""
+    if type(Nd) != tuple:
+        raise TypeError('Nd must be tuple, e.g. (256, 256)')
+    if type(Kd) != tuple:
+        raise TypeError('Kd must be tuple, e.g. (512, 512)')
+    if type(Jd) != tuple:
+        raise TypeError('Jd must be tuple, e.g. (6, 6)')
+    if len(Nd) != len(Kd) or len(Nd) != len(Jd):
+        raise KeyError('Nd, Kd, Jd must be in the same length, e.g. '
+                       'Nd=(256,256),Kd=(512,512),Jd=(6,6)')
+
+
+# --------------------------------------------------------------------------
+# the operator
+# --------------------------------------------------------------------------
+class OracleNUFFT:
+    """numpy restatement of the reference ``NUFFT`` CPU backend
+    (nufft/_nufft_class_methods_cpu.py:27-362).
+
+    ``batch`` follows the deprecated device class (linalg/nufft_hsa.py:203-228):
+    x is Nd+(B,), k is Kd+(B,), y is (M,B); each coil is an independent
+    single-coil transform sharing the plan.
+    """
+
+    def plan(self, om, Nd, Kd, Jd, batch=None, threads=1):
+        check_plan_args(Nd, Kd, Jd)
+        self.Nd, self.Kd, self.Jd = Nd, Kd, Jd
+        self.ndims = len(Nd)
+        self.batch = batch
+        self.threads = int(threads)
+        om = np.asarray(om, dtype=np.float64)
+        self.M = om.shape[0]
+        self.params = [alpha_beta_fit(Nd[i], Jd[i], Kd[i]) for i in range(self.ndims)]
+        self.snd = [scale_axis(Nd[i], Kd[i], *self.params[i]) for i in range(self.ndims)]
+        sn = np.ones(())
+        for i, s in enumerate(self.snd):
+            shp = [1] * self.ndims
+            shp[i] = s.size
+            sn = sn * s.reshape(shp)
+        self.sn = np.asarray(sn.real.astype(np.complex64), order='C')
+        self.sp = interp_csr(om, Nd, Kd, Jd, self.params)
+        self.spH = self.sp.getH().tocsr()
+        self._row_chunks = None
+        return 0
+
+    # ---- helpers for the (optional) threaded sparse products -------------
+    def _chunks(self, n):
+        t = max(1, self.threads)
+        edges = np.linspace(0, n, t + 1).astype(np.int64)
+        return [(int(a), int(b)) for a, b in zip(edges[:-1], edges[1:]) if b > a]
+
+    def _matvec(self, A, v):
+        if self.threads <= 1:
+            return A.dot(v)
+        out = np.empty(A.shape[0], dtype=np.result_type(A.dtype, v.dtype))
+        chunks = self._chunks(A.shape[0])
+        with ThreadPoolExecutor(len(chunks)) as ex:
+            def work(ab):
+                a, b = ab
+                out[a:b] = A[a:b].dot(v)
+            list(ex.map(work, chunks))
+        return out
+
+    def _fftn(self, a, inverse=False):
+        if self.threads <= 1:
+            return np.fft.ifftn(a) if inverse else np.fft.fftn(a)
+        import scipy.fft
+        f = scipy.fft.ifftn if inverse else scipy.fft.fftn
+        return f(a, workers=self.threads)
+
+    # ---- single-coil stages (nufft/_nufft_class_methods_cpu.py) -----------
+    def _x2xx1(self, x):              # :224-230
+        return x * self.sn
+
+    def _xx2k1(self, xx):             # :232-249 (+ preindex_copy, helper.py:830-881)
+        out = np.zeros(self.Kd, dtype=np.complex64)
+        out[tuple(slice(0, n) for n in self.Nd)] = xx
+        return self._fftn(out)
+
+    def _k2y1(self, k):               # :273-288
+        return self._matvec(self.sp, np.reshape(k, (-1,)))
+
+    def _y2k1(self, y):               # :290-314
+        return np.reshape(self._matvec(self.spH, y), self.Kd)
+
+    def _k2xx1(self, k):              # :316-329
+        k = self._fftn(k, inverse=True)
+        xx = np.zeros(self.Nd, dtype=np.complex64)
+        xx[...] = k[tuple(slice(0, n) for n in self.Nd)]
+        return xx
+
+    # ---- batch-aware public stages ----------------------------------------
+    def _per_coil(self, fn, a, lead_shape):
+        if self.batch is None:
+            return fn(a)
+        outs = [fn(a[..., b]) for b in range(a.shape[-1])]
+        return np.stack(outs, axis=-1)
+
+    def x2xx(self, x):
+        if self.batch is None:
+            return self._x2xx1(x)
+        return x * self.sn[..., None]
+
+    def xx2x(self, xx):               # :346-351 (same multiply as x2xx)
+        return self.x2xx(xx)
+
+    def xx2k(self, xx):
+        return self._per_coil(self._xx2k1, xx, self.Nd)
+
+    def k2y(self, k):
+        return self._per_coil(self._k2y1, k, self.Kd)
+
+    def y2k(self, y):
+        return self._per_coil(self._y2k1, y, (self.M,))
+
+    def k2xx(self, k):
+        return self._per_coil(self._k2xx1, k, self.Kd)
+
+    def forward(self, x):             # :168-179
+        return self.k2y(self.xx2k(self.x2xx(x)))
+
+    def adjoint(self, y):             # :181-193
+        return self.xx2x(self.k2xx(self.y2k(y)))
+
+    def k2y2k(self, k):               # :353-362
+        return self.y2k(self.k2y(k))
+
+    def selfadjoint(self, x):         # :201-214
+        return self.xx2x(self.k2xx(self.k2y2k(self.xx2k(self.x2xx(x)))))
+
+    def solve(self, y, solver='cg', maxiter=None, rtol=1e-5, atol=0.0,
+              return_info=False):
+        """solve(y, 'cg', maxiter): CG on the k-space normal operator spH.sp,
+        x0 = 0, then k2xx(k) / sn (linalg/solve_cpu.py:256-288).  The CG
+        recursion restates scipy.sparse.linalg.cg (scipy 1.18.1,
+        sparse/linalg/_isolve/iterative.py) without a preconditioner."""
+        if solver != 'cg':
+            raise NotImplementedError(solver)
+
+        def one(yc):
+            b = np.reshape(self._y2k1(yc), (-1,))
+            x, it = cg_restated(lambda v: self._matvec(self.spH, self._matvec(self.sp, v)),
+                                b, maxiter=maxiter, rtol=rtol, atol=atol)
+            xx = self._k2xx1(np.reshape(x, self.Kd))
+            return xx / self.sn, it
+
+        if self.batch is None:
+            x, it = one(y)
+            return (x, it) if return_info else x
+        outs = [one(y[:, b]) for b in range(y.shape[1])]
+        x = np.stack([o[0] for o in outs], axis=-1)
+        return (x, [o[1] for o in outs]) if return_info else x
+
+
+def cg_restated(matvec, b, maxiter=None, rtol=1e-5, atol=0.0):
+    """Conjugate gradients with scipy.sparse.linalg.cg's recursion and stopping
+    rule (x0 = 0; stop when ||r|| < max(atol, rtol*||b||) at the top of an
+    iteration).  Returns (x, iterations_run)."""
+    b = np.asarray(b)
+    bnrm2 = np.linalg.norm(b)
+    tol = max(float(atol), float(rtol) * float(bnrm2))
+    x = np.zeros_like(b)
+    if bnrm2 == 0:
+        return b, 0
+    if maxiter is None:
+        maxiter = b.size * 10
+    r = b.copy()
+    rho_prev = None
+    p = None
+    for it in range(maxiter):
+        if np.linalg.norm(r) < tol:
+            return x, it
+        rho = np.vdot(r, r)
+        if it > 0:
+            p = r + (rho / rho_prev) * p
+        else:
+            p = r.copy()
+        q = matvec(p)
+        alpha = rho / np.vdot(p, q)
+        x = x + alpha * p
+        r = r - alpha * q
+        rho_prev = rho
+    return x, maxiter
+
+
+# --------------------------------------------------------------------------
+# exact NUDFT on subsets (linalg/nudft_cpu.py:27-41, 92-103)
+# --------------------------------------------------------------------------
+def _centred_grid(Nd):
+    return [np.arange(n, dtype=np.float64) - n / 2 for n in Nd]
+
+
+def nudft_forward_rows(x, om, rows=None):
+    """y_m = sum_n x_n exp(-i om_m . (n - N/2)) for the selected rows, FP64.
+    Separable per axis, so memory is O(rows * sum(Nd))."""
+    x = np.asarray(x, dtype=np.complex128)
+    om = np.asarray(om, dtype=np.float64)
+    if rows is not None:
+        om = om[np.asarray(rows)]
+    Nd = x.shape
+    grids = _centred_grid(Nd)
+    F = [np.exp(-1j * np.outer(om[:, d], grids[d])) for d in range(len(Nd))]
+    out = np.empty(om.shape[0], dtype=np.complex128)
+    for s in range(0, om.shape[0], 256):
+        e = min(om.shape[0], s + 256)
+        t = x
+        # contract the last axis first, keeping the point axis in front
+        t = np.einsum('...n,mn->m...', t, F[-1][s:e])
+        for d in range(len(Nd) - 2, -1, -1):
+            t = np.einsum('m...n,mn->m...', t, F[d][s:e])
+        out[s:e] = t
+    return out
+
+
+def nudft_adjoint_pixels(y, om, Nd, pixels, chunk=65536):
+    """x_n = sum_m y_m exp(+i om_m . (n - N/2)) at the selected flat pixel
+    indices (C order), FP64, unnormalised, summed over chunks of points.  The
+    reference NUFFT adjoint equals this divided by prod(Kd)."""
+    y = np.asarray(y, dtype=np.complex128)
+    om = np.asarray(om, dtype=np.float64)
+    idx = np.unravel_index(np.asarray(pixels), Nd)
+    cen = np.stack([idx[d] - Nd[d] / 2 for d in range(len(Nd))], 1)   # P x d
+    out = np.zeros(len(pixels), dtype=np.complex128)
+    for s in range(0, om.shape[0], chunk):
+        e = min(om.shape[0], s + chunk)
+        out += np.exp(1j * (cen @ om[s:e].T)) @ y[s:e]
+    return out
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a).astype(np.complex128).ravel()
+    b = np.asarray(b).astype(np.complex128).ravel()
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))

@@ -1,0 +1,342 @@
+// extern "C" entry points of libpynufft_gb300.so (declared in
+// include/pynufft_gb300.h).  Each one validates its plan, then queues work on
+// the caller's stream; nothing here synchronises except nufft_set_points and
+// nufft_solve_cg when iteration counts are requested.
+#include "nufft_internal.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+namespace nufft {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+}  // namespace nufft
+
+using namespace nufft;
+
+nufft::Geom nufft_plan_s::geom() const {
+    Geom g{};
+    g.ndim = ndim;
+    g.B = B;
+    for (int d = 0; d < 3; ++d) {
+        g.K[d] = Kd[d];
+        g.J[d] = (d < ndim) ? Jd[d] : 1;
+        g.JP[d] = (d < ndim) ? ((Jd[d] + 1) & ~1) : 0;
+        g.bs[d] = (d < ndim) ? bs[d] : 1;
+        g.nb[d] = (d < ndim && bs[d] > 0) ? (Kd[d] + bs[d] - 1) / bs[d] : 1;
+        g.T[d] = (d < ndim) ? bs[d] + Jd[d] - 1 : 1;
+    }
+    g.prodK = prodK;
+    int64_t nbi = 1;
+    for (int d = 0; d < ndim; ++d) nbi *= g.nb[d];
+    g.nbin_inst = nbi;
+    g.M = M;
+    g.ninst = ninst;
+    g.inst_start = d_inst_start;
+    g.perm = d_perm;
+    int64_t Ma = std::max<int64_t>(M, 1);
+    const float2* c = d_coef;
+    for (int d = 0; d < 3; ++d) {
+        g.pos[d] = (d < ndim && d_pos) ? d_pos + (size_t)d * Ma : nullptr;
+        g.coef[d] = (d < ndim) ? c : nullptr;
+        if (d < ndim && c) c += (size_t)Ma * g.JP[d];
+    }
+    g.sub = d_sub;
+    g.nsub = nsub;
+    return g;
+}
+
+static inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+static int need_plan(nufft_plan_t p, const char* fn) {
+    if (!p) {
+        set_error(std::string(fn) + ": plan is NULL");
+        return NUFFT_EINVAL;
+    }
+    return NUFFT_OK;
+}
+
+static int need_points(nufft_plan_t p, const char* fn) {
+    NUFFT_TRY(need_plan(p, fn));
+    if (!p->d_perm) {
+        set_error(std::string(fn) + ": nufft_set_points has not been called");
+        return NUFFT_ENOPOINTS;
+    }
+    return NUFFT_OK;
+}
+
+// Data pointers may be NULL only for arrays with no elements (an empty
+// trajectory gives empty y arrays).
+static int need_ptrs(const void* a, const void* b, const char* fn, const nufft_plan_s* p = nullptr) {
+    const bool empty_ok = p && p->M == 0;
+    if ((!a || !b) && !empty_ok) {
+        set_error(std::string(fn) + ": NULL data pointer");
+        return NUFFT_EINVAL;
+    }
+    return NUFFT_OK;
+}
+
+extern "C" {
+
+const char* nufft_last_error(void) { return g_last_error.c_str(); }
+
+const char* nufft_version(void) { return "pynufft_gb300 0.1.0 (sm_103a)"; }
+
+int nufft_plan_create(int ndim, const int* Nd, const int* Kd, const int* Jd, int batch, int ninst,
+                      int flags, nufft_plan_t* plan_out) {
+    if (!plan_out || !Nd || !Kd || !Jd) {
+        set_error("nufft_plan_create: NULL argument");
+        return NUFFT_EINVAL;
+    }
+    *plan_out = nullptr;
+    if (ndim < 1 || ndim > NUFFT_MAXDIM) {
+        set_error("nufft_plan_create: ndim must be 1, 2 or 3");
+        return NUFFT_EUNSUPPORTED;
+    }
+    if (batch < 1 || ninst < 1) {
+        set_error("nufft_plan_create: batch and ninst must be >= 1");
+        return NUFFT_EINVAL;
+    }
+    nufft_plan_s* p = new nufft_plan_s();
+    p->ndim = ndim;
+    p->B = batch;
+    p->ninst = ninst;
+    p->flags = flags;
+    int64_t sumN = 0;
+    for (int d = 0; d < ndim; ++d) {
+        if (Nd[d] < 1 || Kd[d] < 1 || Jd[d] < 1 || Nd[d] > Kd[d] || Jd[d] > Kd[d] ||
+            Jd[d] > NUFFT_MAXJ) {
+            set_error("nufft_plan_create: need 1 <= Nd <= Kd, 1 <= Jd <= min(Kd, 16) on every axis");
+            delete p;
+            return NUFFT_EINVAL;
+        }
+        p->Nd[d] = Nd[d];
+        p->Kd[d] = Kd[d];
+        p->Jd[d] = Jd[d];
+        p->prodN *= Nd[d];
+        p->prodK *= Kd[d];
+        sumN += Nd[d];
+        int st = axis_params(Nd[d], Jd[d], Kd[d], p->ax[d]);
+        if (st != NUFFT_OK) {
+            set_error("nufft_plan_create: axis parameters");
+            delete p;
+            return st;
+        }
+    }
+    if ((int64_t)ninst * p->prodK * batch >= ((int64_t)1 << 40)) {
+        set_error("nufft_plan_create: grid too large");
+        delete p;
+        return NUFFT_EINVAL;
+    }
+    auto fail = [&](int st) {
+        nufft_plan_destroy(p);
+        return st;
+    };
+    if (cudaGetDevice(&p->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess) {
+        set_error("nufft_plan_create: no CUDA device");
+        return fail(NUFFT_ECUDA);
+    }
+    std::vector<float> snd(sumN);
+    int64_t off = 0;
+    for (int d = 0; d < ndim; ++d)
+        for (int n = 0; n < Nd[d]; ++n) snd[off++] = (float)p->ax[d].sn[n];
+    cudaError_t e;
+    e = cudaMalloc(&p->d_snd, sizeof(float) * sumN);
+    if (e == cudaSuccess) e = cudaMemcpy(p->d_snd, snd.data(), sizeof(float) * sumN, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_axc, sizeof(AxisConst) * 3);
+    const size_t ncell = (size_t)ninst * p->prodK * batch;
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_grid, sizeof(float2) * ncell);
+    if (e != cudaSuccess) {
+        set_error(std::string("nufft_plan_create: ") + cudaGetErrorString(e));
+        return fail(e == cudaErrorMemoryAllocation ? NUFFT_ENOMEM : NUFFT_ECUDA);
+    }
+    p->dev_bytes = sizeof(float) * sumN + sizeof(AxisConst) * 3 + sizeof(float2) * ncell;
+    int st = fft_init(p);
+    if (st != NUFFT_OK) return fail(st);
+    *plan_out = p;
+    return NUFFT_OK;
+}
+
+int nufft_plan_destroy(nufft_plan_t p) {
+    if (!p) return NUFFT_OK;
+    free_points(p);
+    free_cg(p);
+    if (p->fft_ok) cufftDestroy(p->fft);
+    cudaFree(p->d_snd);
+    cudaFree(p->d_axc);
+    cudaFree(p->d_grid);
+    cudaFree(p->d_igrid);
+    cudaFree(p->d_dscal);
+    delete p;
+    return NUFFT_OK;
+}
+
+int nufft_plan_set_alpha(nufft_plan_t p, int axis, const float* alpha, int L) {
+    NUFFT_TRY(need_plan(p, "nufft_plan_set_alpha"));
+    if (axis < 0 || axis >= p->ndim || !alpha || L < 0 || L > NUFFT_MAXL) {
+        set_error("nufft_plan_set_alpha: need 0 <= axis < ndim, alpha != NULL, 0 <= L <= 14");
+        return NUFFT_EINVAL;
+    }
+    AxisParams& ap = p->ax[axis];
+    ap.L = L;
+    for (int l = 0; l < NUFFT_NALPHA; ++l) ap.alpha[l] = (l <= L) ? alpha[l] : 0.f;
+    NUFFT_TRY(derive_axis(ap));
+    int off = 0;
+    for (int d = 0; d < axis; ++d) off += p->Nd[d];
+    std::vector<float> snd(p->Nd[axis]);
+    for (int n = 0; n < p->Nd[axis]; ++n) snd[n] = (float)ap.sn[n];
+    NUFFT_CUDA_TRY(cudaMemcpy(p->d_snd + off, snd.data(), sizeof(float) * snd.size(),
+                              cudaMemcpyHostToDevice));
+    // tables built from the old coefficients are stale
+    free_cg(p);
+    free_points(p);
+    return NUFFT_OK;
+}
+
+int nufft_set_points(nufft_plan_t p, const int64_t* counts, const double* om, int om_on_device,
+                     void* stream) {
+    NUFFT_TRY(need_plan(p, "nufft_set_points"));
+    free_cg(p);
+    return set_points(p, counts, om, om_on_device, as_stream(stream));
+}
+
+int nufft_plan_set_bins(nufft_plan_t p, const int* bin_shape, int max_sub_points) {
+    NUFFT_TRY(need_plan(p, "nufft_plan_set_bins"));
+    if (bin_shape)
+        for (int d = 0; d < p->ndim; ++d) {
+            if (bin_shape[d] < 0) {
+                set_error("nufft_plan_set_bins: negative bin size");
+                return NUFFT_EINVAL;
+            }
+            p->user_bs[d] = bin_shape[d];
+        }
+    if (max_sub_points < 0) {
+        set_error("nufft_plan_set_bins: negative max_sub_points");
+        return NUFFT_EINVAL;
+    }
+    p->user_maxsub = max_sub_points;
+    return NUFFT_OK;
+}
+
+int nufft_plan_info(nufft_plan_t p, int64_t* M_total, int64_t* n_sub, int64_t* device_bytes) {
+    NUFFT_TRY(need_plan(p, "nufft_plan_info"));
+    if (M_total) *M_total = p->M;
+    if (n_sub) *n_sub = p->nsub;
+    if (device_bytes) {
+        int64_t pts = 0;
+        if (p->d_perm) {
+            int64_t Ma = std::max<int64_t>(p->M, 1);
+            pts = Ma * 4 * (1 + p->ndim);
+            for (int d = 0; d < p->ndim; ++d) pts += Ma * ((p->Jd[d] + 1) & ~1) * 8;
+            pts += (int64_t)p->ybuf_elems * 8 + p->nsub * 16;
+        }
+        *device_bytes = (int64_t)p->dev_bytes + pts;
+    }
+    return NUFFT_OK;
+}
+
+int nufft_x2xx(nufft_plan_t p, const void* x, void* xx, void* stream) {
+    NUFFT_TRY(need_plan(p, "nufft_x2xx"));
+    NUFFT_TRY(need_ptrs(x, xx, "nufft_x2xx"));
+    return launch_scale(p, (const float2*)x, (float2*)xx, as_stream(stream));
+}
+
+int nufft_xx2x(nufft_plan_t p, const void* xx, void* x, void* stream) {
+    NUFFT_TRY(need_plan(p, "nufft_xx2x"));
+    NUFFT_TRY(need_ptrs(x, xx, "nufft_xx2x"));
+    return launch_scale(p, (const float2*)xx, (float2*)x, as_stream(stream));
+}
+
+int nufft_xx2k(nufft_plan_t p, const void* xx, void* k, void* stream) {
+    NUFFT_TRY(need_plan(p, "nufft_xx2k"));
+    NUFFT_TRY(need_ptrs(xx, k, "nufft_xx2k"));
+    cudaStream_t s = as_stream(stream);
+    NUFFT_TRY(launch_pad(p, (const float2*)xx, (float2*)k, false, -1, s));
+    return fft_exec(p, (float2*)k, -1, s);
+}
+
+int nufft_k2xx(nufft_plan_t p, const void* k, void* xx, void* stream) {
+    NUFFT_TRY(need_plan(p, "nufft_k2xx"));
+    NUFFT_TRY(need_ptrs(k, xx, "nufft_k2xx"));
+    cudaStream_t s = as_stream(stream);
+    const size_t n = (size_t)p->ninst * p->prodK * p->B;
+    NUFFT_CUDA_TRY(cudaMemcpyAsync(p->d_grid, k, sizeof(float2) * n, cudaMemcpyDeviceToDevice, s));
+    NUFFT_TRY(fft_exec(p, p->d_grid, +1, s));
+    return launch_crop(p, p->d_grid, (float2*)xx, false, false, s);
+}
+
+int nufft_k2y(nufft_plan_t p, const void* k, void* y, void* stream) {
+    NUFFT_TRY(need_points(p, "nufft_k2y"));
+    NUFFT_TRY(need_ptrs(k, y, "nufft_k2y", p));
+    return launch_k2y(p, (const float2*)k, (float2*)y, as_stream(stream));
+}
+
+int nufft_y2k(nufft_plan_t p, const void* y, void* k, void* stream) {
+    NUFFT_TRY(need_points(p, "nufft_y2k"));
+    NUFFT_TRY(need_ptrs(y, k, "nufft_y2k", p));
+    return launch_y2k(p, (const float2*)y, (float2*)k, as_stream(stream));
+}
+
+int nufft_forward(nufft_plan_t p, const void* x, void* y, void* stream) {
+    NUFFT_TRY(need_points(p, "nufft_forward"));
+    NUFFT_TRY(need_ptrs(x, y, "nufft_forward", p));
+    cudaStream_t s = as_stream(stream);
+    NUFFT_TRY(launch_pad(p, (const float2*)x, p->d_grid, true, -1, s));
+    NUFFT_TRY(fft_exec(p, p->d_grid, -1, s));
+    return launch_k2y(p, p->d_grid, (float2*)y, s);
+}
+
+int nufft_adjoint(nufft_plan_t p, const void* y, void* x, void* stream) {
+    NUFFT_TRY(need_points(p, "nufft_adjoint"));
+    NUFFT_TRY(need_ptrs(x, y, "nufft_adjoint", p));
+    cudaStream_t s = as_stream(stream);
+    NUFFT_TRY(launch_y2k(p, (const float2*)y, p->d_grid, s));
+    NUFFT_TRY(fft_exec(p, p->d_grid, +1, s));
+    return launch_crop(p, p->d_grid, (float2*)x, true, false, s);
+}
+
+int nufft_selfadjoint(nufft_plan_t p, const void* x, void* x_out, void* stream) {
+    NUFFT_TRY(need_points(p, "nufft_selfadjoint"));
+    NUFFT_TRY(need_ptrs(x, x_out, "nufft_selfadjoint"));
+    NUFFT_TRY(nufft_forward(p, x, p->d_ybuf, stream));
+    return nufft_adjoint(p, p->d_ybuf, x_out, stream);
+}
+
+int nufft_k2y2k(nufft_plan_t p, const void* k, void* k_out, void* stream) {
+    NUFFT_TRY(need_points(p, "nufft_k2y2k"));
+    NUFFT_TRY(need_ptrs(k, k_out, "nufft_k2y2k"));
+    cudaStream_t s = as_stream(stream);
+    NUFFT_TRY(launch_k2y(p, (const float2*)k, p->d_ybuf, s));
+    return launch_y2k(p, p->d_ybuf, (float2*)k_out, s);
+}
+
+int nufft_solve_cg(nufft_plan_t p, const void* y, void* x, int maxiter, double rtol, double atol,
+                   int* iters_out, void* stream) {
+    NUFFT_TRY(need_points(p, "nufft_solve_cg"));
+    NUFFT_TRY(need_ptrs(y, x, "nufft_solve_cg", p));
+    if (!(rtol >= 0) || !(atol >= 0)) {
+        set_error("nufft_solve_cg: rtol and atol must be non-negative");
+        return NUFFT_EINVAL;
+    }
+    return solve_cg(p, (const float2*)y, (float2*)x, maxiter, rtol, atol, iters_out,
+                    as_stream(stream));
+}
+
+int nufft_forward_dom(nufft_plan_t p, const void* x, void* dy, void* stream) {
+    NUFFT_TRY(need_points(p, "nufft_forward_dom"));
+    NUFFT_TRY(need_ptrs(x, dy, "nufft_forward_dom", p));
+    cudaStream_t s = as_stream(stream);
+    const size_t stride = (size_t)p->M * p->B;
+    for (int d = 0; d < p->ndim; ++d) {
+        NUFFT_TRY(launch_pad(p, (const float2*)x, p->d_grid, true, d, s));
+        NUFFT_TRY(fft_exec(p, p->d_grid, -1, s));
+        NUFFT_TRY(launch_k2y(p, p->d_grid, (float2*)dy + d * stride, s));
+    }
+    return NUFFT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,141 @@
+// Launchers for the interpolation (k2y) and gridding (y2k) kernels, and the
+// fixed-point helpers of the deterministic gridding mode.  The kernel
+// instantiations live in interp_d1.cu / interp_d2.cu / interp_d3.cu.
+#include "nufft_internal.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+namespace nufft {
+
+void k2y_dim1(int jm, const Geom& g, const float2* grid, float2* y, cudaStream_t s);
+void k2y_dim2(int jm, const Geom& g, const float2* grid, float2* y, cudaStream_t s);
+void k2y_dim3(int jm, const Geom& g, const float2* grid, float2* y, cudaStream_t s);
+int y2k_dim1(int jm, bool det, const Geom& g, const float2* y, float2* grid,
+             unsigned long long* igrid, const double* dscal, cudaStream_t s);
+int y2k_dim2(int jm, bool det, const Geom& g, const float2* y, float2* grid,
+             unsigned long long* igrid, const double* dscal, cudaStream_t s);
+int y2k_dim3(int jm, bool det, const Geom& g, const float2* y, float2* grid,
+             unsigned long long* igrid, const double* dscal, cudaStream_t s);
+
+static int pick_jm(const nufft_plan_s* p) {
+    int j = 1;
+    for (int d = 0; d < p->ndim; ++d) j = std::max(j, p->Jd[d]);
+    if (j <= 4) return 4;
+    if (j <= 6) return 6;
+    if (j <= 8) return 8;
+    return 16;
+}
+
+// ---------------------------------------------------------------------------
+// k2y
+// ---------------------------------------------------------------------------
+int launch_k2y(const nufft_plan_s* p, const float2* grid, float2* y, cudaStream_t s) {
+    if (p->M == 0) return NUFFT_OK;
+    Geom g = p->geom();
+    const int jm = pick_jm(p);
+    switch (p->ndim) {
+        case 1: k2y_dim1(jm, g, grid, y, s); break;
+        case 2: k2y_dim2(jm, g, grid, y, s); break;
+        default: k2y_dim3(jm, g, grid, y, s); break;
+    }
+    return check_launch("k2y_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// y2k
+// ---------------------------------------------------------------------------
+// Sum over all samples and coils of |re| + |im|, reduced in a fixed order
+// (per-block partials, then one block), so the fixed-point scale derived from
+// it is itself reproducible.
+__global__ void abs_sum_partial_kernel(const float2* __restrict__ y, int64_t n,
+                                       double* __restrict__ part) {
+    __shared__ double red[256];
+    double acc = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float2 v = y[i];
+        acc += (double)(fabsf(v.x) + fabsf(v.y));
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// dscal[1] = 2^(62 - e) with 2^e >= 1.01 * wmax * sum|y|: every partial sum of
+// fixed-point contributions stays below 2^62 in magnitude.
+__global__ void fixed_scale_kernel(const double* __restrict__ part, int nparts, float wmax,
+                                   double* __restrict__ dscal) {
+    __shared__ double red[256];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc += part[i];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double bound = 1.01 * (double)wmax * red[0];
+        int e = 0;
+        if (bound > 0 && isfinite(bound)) e = (int)ceil(log2(bound));
+        dscal[0] = red[0];
+        dscal[1] = ldexp(1.0, 62 - e);
+    }
+}
+
+__global__ void fixed_to_float_kernel(const unsigned long long* __restrict__ ig, int64_t n,
+                                      const double* __restrict__ dscal, float2* __restrict__ out) {
+    const float inv = (float)(1.0 / dscal[1]);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const long long a = (long long)ig[2 * i], b = (long long)ig[2 * i + 1];
+        out[i] = make_float2(__ll2float_rn(a) * inv, __ll2float_rn(b) * inv);
+    }
+}
+
+template <bool DET>
+static int y2k_dim(const nufft_plan_s* p, const Geom& g, const float2* y, float2* grid,
+                   unsigned long long* igrid, const double* dscal, cudaStream_t s) {
+    const int jm = pick_jm(p);
+    switch (p->ndim) {
+        case 1: return y2k_dim1(jm, DET, g, y, grid, igrid, dscal, s);
+        case 2: return y2k_dim2(jm, DET, g, y, grid, igrid, dscal, s);
+        default: return y2k_dim3(jm, DET, g, y, grid, igrid, dscal, s);
+    }
+}
+
+int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s) {
+    const size_t ncells = (size_t)p->ninst * p->prodK * p->B;
+    Geom g = p->geom();
+    if (!(p->flags & NUFFT_FLAG_DETERMINISTIC)) {
+        NUFFT_CUDA_TRY(cudaMemsetAsync(grid, 0, sizeof(float2) * ncells, s));
+        if (p->M == 0) return NUFFT_OK;
+        return y2k_dim<false>(p, g, y, grid, nullptr, nullptr, s);
+    }
+    // deterministic: exact fixed-point accumulation, then one rounding to float
+    if (!p->d_igrid) {
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_igrid, sizeof(unsigned long long) * 2 * ncells));
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_dscal, sizeof(double) * (2 + 1024)));
+        p->dev_bytes += sizeof(unsigned long long) * 2 * ncells + sizeof(double) * 1026;
+    }
+    NUFFT_CUDA_TRY(cudaMemsetAsync(p->d_igrid, 0, sizeof(unsigned long long) * 2 * ncells, s));
+    const int64_t ny = p->M * (int64_t)p->B;
+    const int nparts = 1024;
+    double* part = p->d_dscal + 2;
+    abs_sum_partial_kernel<<<nparts, 256, 0, s>>>(y, ny, part);
+    NUFFT_TRY(check_launch("abs_sum_partial_kernel"));
+    fixed_scale_kernel<<<1, 256, 0, s>>>(part, nparts, p->wmax, p->d_dscal);
+    NUFFT_TRY(check_launch("fixed_scale_kernel"));
+    if (p->M > 0) NUFFT_TRY(y2k_dim<true>(p, g, y, nullptr, p->d_igrid, p->d_dscal, s));
+    const int blocks = (int)std::min<size_t>((ncells + 255) / 256, (size_t)p->num_sms * 16);
+    fixed_to_float_kernel<<<std::max(blocks, 1), 256, 0, s>>>(p->d_igrid, (int64_t)ncells,
+                                                               p->d_dscal, grid);
+    return check_launch("fixed_to_float_kernel");
+}
+
+}  // namespace nufft

@@ -1,0 +1,176 @@
+// Internal definitions shared by the pynufft_gb300 CUDA sources.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/pynufft_gb300.h"
+
+#define NUFFT_MAXDIM 3
+#define NUFFT_MAXJ 16
+#define NUFFT_MAXL 14     // L = ceil(N/3) reaches 14 at N = 40
+#define NUFFT_NALPHA 16   // coefficient array length (>= MAXL + 1)
+
+namespace nufft {
+
+void set_error(const std::string& msg);
+
+// Plan-time numerics of one axis (plan_math.cpp).
+struct AxisParams {
+    int N = 0, J = 0, K = 0, L = 0;
+    float alpha[NUFFT_NALPHA];
+    std::vector<double> sn;  // N
+    std::vector<double> T;   // J*J, row major
+};
+int axis_params(int N, int J, int K, AxisParams& ap);
+int derive_axis(AxisParams& ap);  // sn and T from N, J, K, L, alpha
+
+// Constants of one axis used by the per-point table kernel (points.cu).
+struct AxisConst {
+    double gam;          // 2 pi / K
+    double inv_ratio;    // N / K
+    double lin;          // gam * (N - 1) / 2
+    double half_N;       // N / 2
+    int K, J, L, N;
+    double alpha[NUFFT_MAXL + 1];
+    double T[NUFFT_MAXJ * NUFFT_MAXJ];
+};
+
+// Everything a gather/scatter kernel needs, passed by value.
+struct Geom {
+    int ndim;
+    int B;                    // coils (batch), fastest axis of x/k/y
+    int K[3], J[3], JP[3];    // grid size, neighbours, table stride (J rounded up to even)
+    int bs[3], nb[3];         // bin shape and bins per axis
+    int T[3];                 // scatter tile extent per axis = bs + J - 1
+    int64_t prodK;            // cells per instance
+    int64_t nbin_inst;        // bins per instance
+    int64_t M;                // total points
+    int ninst;
+    const int64_t* inst_start;   // ninst+1 prefix of points per instance (device)
+    const int* perm;             // sorted -> original point index
+    const int* pos[3];           // first footprint index per axis, sorted order
+    const float2* coef[3];       // conj(u) coefficients, sorted order, stride JP
+    const int4* sub;             // gridding sub-problems: (bin, start, count, inst)
+    int64_t nsub;
+};
+
+}  // namespace nufft
+
+struct nufft_plan_s {
+    int ndim = 0;
+    int Nd[3] = {1, 1, 1}, Kd[3] = {1, 1, 1}, Jd[3] = {1, 1, 1};
+    int B = 1, ninst = 1, flags = 0;
+    int64_t prodN = 1, prodK = 1;
+    nufft::AxisParams ax[3];
+    int bs[3] = {0, 0, 0};
+    int user_bs[3] = {0, 0, 0};
+    int maxsub = 0, user_maxsub = 0;
+    int device = 0;
+    int num_sms = 0;
+
+    // device buffers owned by the plan
+    float* d_snd = nullptr;           // per-axis scaling factors (float32), concatenated
+    nufft::AxisConst* d_axc = nullptr;
+    float2* d_grid = nullptr;         // ninst * prodK * B oversampled grid workspace
+    float2* d_ybuf = nullptr;         // M * B sample workspace (selfadjoint, CG)
+    size_t ybuf_elems = 0;
+
+    // point data (valid after nufft_set_points)
+    int64_t M = 0;
+    std::vector<int64_t> counts;
+    int64_t* d_inst_start = nullptr;
+    int* d_perm = nullptr;
+    int* d_pos = nullptr;             // ndim * M
+    float2* d_coef = nullptr;         // sum_d M * JP[d]
+    int4* d_sub = nullptr;
+    int64_t nsub = 0;
+    int64_t nbins_total = 0;
+    float wmax = 0.f;                 // max over points of prod_d max_j |coef|
+
+    // deterministic gridding
+    unsigned long long* d_igrid = nullptr;  // 2 * ninst * prodK * B fixed-point accumulators
+    double* d_dscal = nullptr;              // [0] = sum |y|, [1] = fixed-point scale
+
+    // CG workspace
+    float2* d_cg = nullptr;           // r, p, q, xk: 4 * ninst * prodK * B
+    double* d_cgs = nullptr;          // device scalars
+    double* d_part = nullptr;         // per-block partial sums
+    int part_blocks = 0;
+    cudaGraphExec_t cg_init_exec = nullptr;   // captured CG set-up (keyed by y, maxiter, tols)
+    cudaGraphExec_t cg_iter_exec = nullptr;   // captured chunk of CG iterations
+    const void* cg_y = nullptr;
+    int cg_maxiter = -1, cg_chunk = 0;
+    double cg_rtol = 0, cg_atol = 0;
+
+    cufftHandle fft = 0;
+    bool fft_ok = false;
+    size_t dev_bytes = 0;
+
+    nufft::Geom geom() const;
+};
+
+namespace nufft {
+
+// error helpers --------------------------------------------------------------
+#define NUFFT_CUDA_TRY(expr)                                                         \
+    do {                                                                             \
+        cudaError_t _e = (expr);                                                     \
+        if (_e != cudaSuccess) {                                                     \
+            ::nufft::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));  \
+            return (_e == cudaErrorMemoryAllocation) ? NUFFT_ENOMEM : NUFFT_ECUDA;   \
+        }                                                                            \
+    } while (0)
+
+#define NUFFT_CUFFT_TRY(expr)                                                        \
+    do {                                                                             \
+        cufftResult _r = (expr);                                                     \
+        if (_r != CUFFT_SUCCESS) {                                                   \
+            ::nufft::set_error(std::string(#expr) + ": cufft error " +               \
+                               std::to_string((int)_r));                             \
+            return NUFFT_ECUFFT;                                                     \
+        }                                                                            \
+    } while (0)
+
+#define NUFFT_TRY(expr)                   \
+    do {                                  \
+        int _s = (expr);                  \
+        if (_s != NUFFT_OK) return _s;    \
+    } while (0)
+
+inline int check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error(std::string(what) + ": " + cudaGetErrorString(e));
+        return NUFFT_ECUDA;
+    }
+    return NUFFT_OK;
+}
+
+// points.cu
+int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_on_device,
+               cudaStream_t s);
+void free_points(nufft_plan_s* p);
+
+// interp.cu
+int launch_k2y(const nufft_plan_s* p, const float2* grid, float2* y, cudaStream_t s);
+int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s);
+
+// fftstage.cu
+int launch_scale(const nufft_plan_s* p, const float2* in, float2* out, cudaStream_t s);
+int launch_pad(const nufft_plan_s* p, const float2* xx, float2* grid, bool apply_sn,
+               int dom_axis, cudaStream_t s);
+int launch_crop(const nufft_plan_s* p, const float2* grid, float2* xx, bool apply_sn,
+                bool divide_sn, cudaStream_t s);
+int fft_exec(nufft_plan_s* p, float2* grid, int direction, cudaStream_t s);
+int fft_init(nufft_plan_s* p);
+
+// cg.cu
+int solve_cg(nufft_plan_s* p, const float2* y, float2* x, int maxiter, double rtol,
+             double atol, int* iters_out, cudaStream_t s);
+void free_cg(nufft_plan_s* p);
+
+}  // namespace nufft

@@ -1,0 +1,404 @@
+// Non-uniform points -> bin-sorted per-axis min-max interpolation tables.
+//
+// This is the GPU counterpart of the interpolator build in helper.plan
+// (src/_helper/helper.py:736-786): instead of the M x prod(Jd) complex128 CSR
+// (full_kron/create_csr, helper.py:449-480, 285-311) it keeps, per axis and per
+// point, the J coefficients conj(u) and the first grid index of the
+// footprint -- the "pELL" idea of helper.py:346-393 -- in bin-sorted order.
+// The Kronecker product of the per-axis tables is formed in registers by the
+// gather/scatter kernels (interp.cu).
+//
+// Pipeline (one stream, one host sync at the end to size the sub-problem list):
+//   1. bin_points      : om -> first footprint index per axis, bin id, rank in bin
+//   2. scan            : bin counts -> bin starts (counting sort)
+//   3. build_tables    : FP64 min-max coefficients (helper.py:606-618,
+//                        1086-1117, 148-162) written at the sorted slot
+//   4. subproblems     : bins split into chunks of <= maxsub points
+#include "nufft_internal.cuh"
+
+#include <cmath>
+#include <algorithm>
+#include <cstring>
+
+namespace nufft {
+
+// ---------------------------------------------------------------------------
+// per-axis constants on the device
+// ---------------------------------------------------------------------------
+struct AxisTab {
+    double cs[2 * NUFFT_MAXL + NUFFT_MAXJ + 2];  // cos(pi n N/K), n = -(L+J) .. L
+    double ss[2 * NUFFT_MAXL + NUFFT_MAXJ + 2];  // sin(pi n N/K)
+};
+
+struct PointsArgs {
+    int ndim;
+    AxisConst ax[3];
+};
+
+__device__ __forceinline__ int inst_of(const int64_t* start, int ninst, int64_t m) {
+    int lo = 0, hi = ninst - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= m) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Step 1: bins.  koff = floor(om/gam - J/2) (nufft_offset, helper.py:900-907);
+// the footprint along an axis is (koff + j) mod K, j = 1..J (OMEGA_k,
+// helper.py:164-210), so its first index is pos = (koff + 1) mod K.
+__global__ void bin_points_kernel(const double* __restrict__ om, int64_t M, int ndim,
+                                  const AxisConst* __restrict__ axc, Geom g,
+                                  int* __restrict__ bin_of, int* __restrict__ rank_of,
+                                  int* __restrict__ bin_count, int* __restrict__ err) {
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
+         m += (int64_t)gridDim.x * blockDim.x) {
+        int inst = (g.ninst > 1) ? inst_of(g.inst_start, g.ninst, m) : 0;
+        int64_t bin = 0;
+        bool ok = true;
+        for (int d = 0; d < ndim; ++d) {
+            double w = om[m * ndim + d];
+            if (!isfinite(w)) { ok = false; break; }
+            const AxisConst& a = axc[d];
+            double t = w / a.gam;
+            double koff = floor(t - a.J * 0.5);
+            double q = koff + 1.0;
+            double r = q - a.K * floor(q / a.K);
+            int pos = (int)r;
+            if (pos >= a.K) pos -= a.K;
+            if (pos < 0) pos += a.K;
+            bin = bin * g.nb[d] + pos / g.bs[d];
+        }
+        if (!ok) {
+            atomicOr(err, 1);
+            bin_of[m] = -1;
+            continue;
+        }
+        bin += (int64_t)inst * g.nbin_inst;
+        bin_of[m] = (int)bin;
+        rank_of[m] = atomicAdd(&bin_count[bin], 1);
+    }
+}
+
+// Exclusive scan of n ints by one block of 1024 threads; out[n] = total.
+__global__ void scan_kernel(const int* __restrict__ in, int* __restrict__ out, int64_t n) {
+    __shared__ long long part[1024];
+    const int tid = threadIdx.x;
+    const int64_t chunk = (n + blockDim.x - 1) / blockDim.x;
+    const int64_t b = tid * chunk, e = min(n, b + chunk);
+    long long s = 0;
+    for (int64_t i = b; i < e; ++i) s += in[i];
+    part[tid] = s;
+    __syncthreads();
+    for (int off = 1; off < blockDim.x; off <<= 1) {
+        long long v = (tid >= off) ? part[tid - off] : 0;
+        __syncthreads();
+        part[tid] += v;
+        __syncthreads();
+    }
+    long long run = part[tid] - s;
+    for (int64_t i = b; i < e; ++i) {
+        out[i] = (int)run;
+        run += in[i];
+    }
+    if (tid == blockDim.x - 1) out[n] = (int)part[tid];
+}
+
+__device__ __forceinline__ double sinc_direct(double x) {
+    if (x == 0.0) return 1.0;
+    return sinpi(x) / (M_PI * x);
+}
+
+// One axis of the min-max interpolator for one point, FP64.
+//   t = om/gam, koff = floor(t - J/2), dk = t - koff, arg_j = dk - j
+//   r_j = sum_l alpha_|l| sinc((arg_j + l)/(K/N))              (nufft_r)
+//   c = T r                                                      (min_max)
+//   u_j = exp(i gam (N-1)/2 arg_j) c_j exp(-i om N/2)            (OMEGA_u)
+//   out_j = conj(u_j)                                            (.T.conj())
+// sin(pi (dk+n) N/K) for |dk+n| >= 1 uses the angle-sum identity with the
+// tabulated sin/cos(pi n N/K); the two terms nearest zero are evaluated
+// directly so the sinc keeps full relative accuracy near its peak.
+__device__ float axis_coefs(const AxisConst& a, const AxisTab& tab, double w,
+                            float2* __restrict__ out) {
+    const int J = a.J, L = a.L;
+    double t = w / a.gam;
+    double koff = floor(t - J * 0.5);
+    double dk = t - koff;
+    double s0, c0;
+    sincospi(dk * a.inv_ratio, &s0, &c0);
+    double r[NUFFT_MAXJ];
+    for (int j = 1; j <= J; ++j) {
+        double acc = 0.0;
+        for (int l = -L; l <= L; ++l) {
+            double xn = dk - j + l;
+            double sv;
+            if (fabs(xn) < 1.0) {
+                sv = sinc_direct(xn * a.inv_ratio);
+            } else {
+                int n = l - j + L + J;
+                double sn = s0 * tab.cs[n] + c0 * tab.ss[n];
+                sv = sn / (M_PI * xn * a.inv_ratio);
+            }
+            acc += a.alpha[l < 0 ? -l : l] * sv;
+        }
+        r[j - 1] = acc;
+    }
+    float amax = 0.f;
+    for (int j = 0; j < J; ++j) {
+        double c = 0.0;
+        for (int i = 0; i < J; ++i) c += a.T[j * J + i] * r[i];
+        double th = a.lin * (dk - (j + 1)) - w * a.half_N;
+        double sth, cth;
+        sincos(th, &sth, &cth);
+        float2 v = make_float2((float)(c * cth), (float)(-c * sth));
+        out[j] = v;
+        amax = fmaxf(amax, sqrtf(v.x * v.x + v.y * v.y));
+    }
+    return amax;
+}
+
+__global__ void build_tables_kernel(const double* __restrict__ om, int64_t M, int ndim,
+                                    const AxisConst* __restrict__ axc,
+                                    const AxisTab* __restrict__ tabs, Geom g,
+                                    const int* __restrict__ bin_of,
+                                    const int* __restrict__ rank_of,
+                                    const int* __restrict__ bin_start,
+                                    int* __restrict__ perm, int* __restrict__ pos,
+                                    float2* __restrict__ coef0, float2* __restrict__ coef1,
+                                    float2* __restrict__ coef2, unsigned int* __restrict__ wmax) {
+    float2* coefs[3] = {coef0, coef1, coef2};
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
+         m += (int64_t)gridDim.x * blockDim.x) {
+        int bin = bin_of[m];
+        if (bin < 0) continue;
+        int64_t s = (int64_t)bin_start[bin] + rank_of[m];
+        perm[s] = (int)m;
+        float wprod = 1.f;
+        for (int d = 0; d < ndim; ++d) {
+            const AxisConst& a = axc[d];
+            double w = om[m * ndim + d];
+            double t = w / a.gam;
+            double koff = floor(t - a.J * 0.5);
+            double q = koff + 1.0;
+            double r = q - a.K * floor(q / a.K);
+            int p = (int)r;
+            if (p >= a.K) p -= a.K;
+            if (p < 0) p += a.K;
+            pos[(int64_t)d * M + s] = p;
+            float2 buf[NUFFT_MAXJ];
+            float amax = axis_coefs(a, tabs[d], w, buf);
+            float2* dst = coefs[d] + s * g.JP[d];
+            for (int j = 0; j < g.JP[d]; ++j) dst[j] = (j < a.J) ? buf[j] : make_float2(0.f, 0.f);
+            wprod *= amax;
+        }
+        atomicMax(wmax, __float_as_uint(wprod));
+    }
+}
+
+__global__ void sub_count_kernel(const int* __restrict__ bin_start, int64_t nbins, int maxsub,
+                                 int* __restrict__ nsub_of) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbins;
+         b += (int64_t)gridDim.x * blockDim.x) {
+        int c = bin_start[b + 1] - bin_start[b];
+        nsub_of[b] = (c + maxsub - 1) / maxsub;
+    }
+}
+
+__global__ void sub_fill_kernel(const int* __restrict__ bin_start, const int* __restrict__ sub_start,
+                                int64_t nbins, int maxsub, int64_t nbin_inst,
+                                int4* __restrict__ sub) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbins;
+         b += (int64_t)gridDim.x * blockDim.x) {
+        int c = bin_start[b + 1] - bin_start[b];
+        int s0 = sub_start[b];
+        for (int k = 0; k * maxsub < c; ++k) {
+            int cnt = min(maxsub, c - k * maxsub);
+            sub[s0 + k] = make_int4((int)b, bin_start[b] + k * maxsub, cnt, (int)(b / nbin_inst));
+        }
+    }
+}
+
+void free_points(nufft_plan_s* p) {
+    cudaFree(p->d_inst_start); p->d_inst_start = nullptr;
+    cudaFree(p->d_perm); p->d_perm = nullptr;
+    cudaFree(p->d_pos); p->d_pos = nullptr;
+    cudaFree(p->d_coef); p->d_coef = nullptr;
+    cudaFree(p->d_sub); p->d_sub = nullptr;
+    cudaFree(p->d_ybuf); p->d_ybuf = nullptr;
+    p->ybuf_elems = 0;
+    p->M = 0;
+    p->nsub = 0;
+}
+
+static void default_bins(const nufft_plan_s* p, int bs[3], int& maxsub) {
+    // cells per bin axis; the scatter tile is (bs + J - 1) per axis
+    for (int d = 0; d < 3; ++d) bs[d] = 1;
+    if (p->ndim == 1) { bs[0] = 1024; maxsub = 1024; }
+    else if (p->ndim == 2) { bs[0] = 32; bs[1] = 32; maxsub = 1024; }
+    else { bs[0] = 8; bs[1] = 8; bs[2] = 8; maxsub = 512; }
+    for (int d = 0; d < p->ndim; ++d) {
+        if (p->user_bs[d] > 0) bs[d] = p->user_bs[d];
+        bs[d] = std::min(bs[d], p->Kd[d]);
+    }
+    if (p->user_maxsub > 0) maxsub = p->user_maxsub;
+}
+
+int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_on_device,
+               cudaStream_t s) {
+    if (!counts) { set_error("nufft_set_points: counts is NULL"); return NUFFT_EINVAL; }
+    int64_t M = 0;
+    for (int i = 0; i < p->ninst; ++i) {
+        if (counts[i] < 0) { set_error("nufft_set_points: negative count"); return NUFFT_EINVAL; }
+        M += counts[i];
+    }
+    if (M >= (int64_t)1 << 31) { set_error("nufft_set_points: more than 2^31-1 points"); return NUFFT_EINVAL; }
+    if (M > 0 && !om) { set_error("nufft_set_points: om is NULL"); return NUFFT_EINVAL; }
+    free_points(p);
+    p->counts.assign(counts, counts + p->ninst);
+    default_bins(p, p->bs, p->maxsub);
+
+    const int nd = p->ndim;
+    int64_t nbin_inst = 1;
+    int nb[3] = {1, 1, 1};
+    for (int d = 0; d < nd; ++d) {
+        nb[d] = (p->Kd[d] + p->bs[d] - 1) / p->bs[d];
+        nbin_inst *= nb[d];
+    }
+    const int64_t nbins = nbin_inst * p->ninst;
+    p->nbins_total = nbins;
+
+    std::vector<int64_t> istart(p->ninst + 1, 0);
+    for (int i = 0; i < p->ninst; ++i) istart[i + 1] = istart[i] + counts[i];
+    NUFFT_CUDA_TRY(cudaMalloc(&p->d_inst_start, sizeof(int64_t) * (p->ninst + 1)));
+    NUFFT_CUDA_TRY(cudaMemcpyAsync(p->d_inst_start, istart.data(), sizeof(int64_t) * (p->ninst + 1),
+                                   cudaMemcpyHostToDevice, s));
+    p->M = M;
+    int64_t Malloc = std::max<int64_t>(M, 1);
+    NUFFT_CUDA_TRY(cudaMalloc(&p->d_perm, sizeof(int) * Malloc));
+    NUFFT_CUDA_TRY(cudaMalloc(&p->d_pos, sizeof(int) * Malloc * nd));
+    int64_t coef_elems = 0;
+    int JP[3] = {0, 0, 0};
+    for (int d = 0; d < nd; ++d) {
+        JP[d] = (p->Jd[d] + 1) & ~1;
+        coef_elems += Malloc * JP[d];
+    }
+    NUFFT_CUDA_TRY(cudaMalloc(&p->d_coef, sizeof(float2) * coef_elems));
+    p->ybuf_elems = (size_t)Malloc * p->B;
+    NUFFT_CUDA_TRY(cudaMalloc(&p->d_ybuf, sizeof(float2) * p->ybuf_elems));
+    NUFFT_CUDA_TRY(cudaMemsetAsync(p->d_ybuf, 0, sizeof(float2) * p->ybuf_elems, s));
+
+    // temporaries
+    double* d_om = nullptr;
+    int *d_bin_of = nullptr, *d_rank = nullptr, *d_cnt = nullptr, *d_start = nullptr;
+    int *d_nsub = nullptr, *d_subst = nullptr, *d_err = nullptr;
+    unsigned int* d_wmax = nullptr;
+    auto cleanup = [&]() {
+        if (!om_on_device) cudaFree(d_om);
+        cudaFree(d_bin_of); cudaFree(d_rank); cudaFree(d_cnt); cudaFree(d_start);
+        cudaFree(d_nsub); cudaFree(d_subst); cudaFree(d_err); cudaFree(d_wmax);
+    };
+#define TRY_TMP(expr)                                                              \
+    do {                                                                           \
+        cudaError_t _e = (expr);                                                   \
+        if (_e != cudaSuccess) {                                                   \
+            set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));         \
+            cleanup();                                                             \
+            return (_e == cudaErrorMemoryAllocation) ? NUFFT_ENOMEM : NUFFT_ECUDA; \
+        }                                                                          \
+    } while (0)
+
+    if (om_on_device) {
+        d_om = const_cast<double*>(om);
+    } else if (M > 0) {
+        TRY_TMP(cudaMalloc(&d_om, sizeof(double) * M * nd));
+        TRY_TMP(cudaMemcpyAsync(d_om, om, sizeof(double) * M * nd, cudaMemcpyHostToDevice, s));
+    }
+    TRY_TMP(cudaMalloc(&d_bin_of, sizeof(int) * Malloc));
+    TRY_TMP(cudaMalloc(&d_rank, sizeof(int) * Malloc));
+    TRY_TMP(cudaMalloc(&d_cnt, sizeof(int) * nbins));
+    TRY_TMP(cudaMalloc(&d_start, sizeof(int) * (nbins + 1)));
+    TRY_TMP(cudaMalloc(&d_nsub, sizeof(int) * nbins));
+    TRY_TMP(cudaMalloc(&d_subst, sizeof(int) * (nbins + 1)));
+    TRY_TMP(cudaMalloc(&d_err, sizeof(int)));
+    TRY_TMP(cudaMalloc(&d_wmax, sizeof(unsigned int)));
+    TRY_TMP(cudaMemsetAsync(d_cnt, 0, sizeof(int) * nbins, s));
+    TRY_TMP(cudaMemsetAsync(d_err, 0, sizeof(int), s));
+    TRY_TMP(cudaMemsetAsync(d_wmax, 0, sizeof(unsigned int), s));
+
+    // per-axis constants (angle tables for the sinc identity)
+    AxisTab htab[3];
+    AxisConst hax[3];
+    for (int d = 0; d < nd; ++d) {
+        const AxisParams& ap = p->ax[d];
+        AxisConst& a = hax[d];
+        a.K = ap.K; a.J = ap.J; a.L = ap.L; a.N = ap.N;
+        a.gam = 2.0 * M_PI / ap.K;
+        a.inv_ratio = (double)ap.N / (double)ap.K;
+        a.lin = a.gam * (ap.N - 1.0) / 2.0;
+        a.half_N = ap.N / 2.0;
+        for (int l = 0; l <= NUFFT_MAXL; ++l) a.alpha[l] = (l <= ap.L) ? (double)ap.alpha[l] : 0.0;
+        for (int i = 0; i < ap.J * ap.J; ++i) a.T[i] = ap.T[i];
+        for (int n = -(ap.L + ap.J); n <= ap.L; ++n) {
+            double ang = M_PI * n * a.inv_ratio;
+            htab[d].cs[n + ap.L + ap.J] = std::cos(ang);
+            htab[d].ss[n + ap.L + ap.J] = std::sin(ang);
+        }
+    }
+    AxisTab* d_tab = nullptr;
+    TRY_TMP(cudaMalloc(&d_tab, sizeof(AxisTab) * 3));
+    TRY_TMP(cudaMemcpyAsync(d_tab, htab, sizeof(AxisTab) * 3, cudaMemcpyHostToDevice, s));
+    TRY_TMP(cudaMemcpyAsync(p->d_axc, hax, sizeof(AxisConst) * 3, cudaMemcpyHostToDevice, s));
+
+    Geom g = p->geom();
+    g.inst_start = p->d_inst_start;
+    const int threads = 256;
+    const int blocks = (int)std::min<int64_t>((M + threads - 1) / threads + 1, 65535 * 8);
+    if (M > 0) {
+        bin_points_kernel<<<blocks, threads, 0, s>>>(d_om, M, nd, p->d_axc, g, d_bin_of, d_rank,
+                                                     d_cnt, d_err);
+        TRY_TMP(cudaGetLastError());
+    }
+    scan_kernel<<<1, 1024, 0, s>>>(d_cnt, d_start, nbins);
+    TRY_TMP(cudaGetLastError());
+    float2* c0 = p->d_coef;
+    float2* c1 = c0 + (nd > 1 ? Malloc * JP[0] : 0);
+    float2* c2 = c1 + (nd > 2 ? Malloc * JP[1] : 0);
+    if (M > 0) {
+        build_tables_kernel<<<blocks, threads, 0, s>>>(d_om, M, nd, p->d_axc, d_tab, g, d_bin_of,
+                                                       d_rank, d_start, p->d_perm, p->d_pos,
+                                                       c0, c1, c2, d_wmax);
+        TRY_TMP(cudaGetLastError());
+    }
+    const int bblocks = (int)std::min<int64_t>((nbins + threads - 1) / threads, 65535);
+    sub_count_kernel<<<bblocks, threads, 0, s>>>(d_start, nbins, p->maxsub, d_nsub);
+    TRY_TMP(cudaGetLastError());
+    scan_kernel<<<1, 1024, 0, s>>>(d_nsub, d_subst, nbins);
+    TRY_TMP(cudaGetLastError());
+    int h_nsub = 0, h_err = 0;
+    unsigned int h_wmax = 0;
+    TRY_TMP(cudaMemcpyAsync(&h_nsub, d_subst + nbins, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TRY_TMP(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TRY_TMP(cudaMemcpyAsync(&h_wmax, d_wmax, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+    TRY_TMP(cudaStreamSynchronize(s));
+    cudaFree(d_tab);
+    if (h_err) {
+        cleanup();
+        free_points(p);
+        set_error("nufft_set_points: om holds NaN or Inf");
+        return NUFFT_EOM_NONFINITE;
+    }
+    std::memcpy(&p->wmax, &h_wmax, sizeof(float));
+    p->nsub = h_nsub;
+    TRY_TMP(cudaMalloc(&p->d_sub, sizeof(int4) * std::max(h_nsub, 1)));
+    if (h_nsub > 0) {
+        sub_fill_kernel<<<bblocks, threads, 0, s>>>(d_start, d_subst, nbins, p->maxsub, nbin_inst,
+                                                    p->d_sub);
+        TRY_TMP(cudaGetLastError());
+    }
+    TRY_TMP(cudaStreamSynchronize(s));
+    cleanup();
+#undef TRY_TMP
+    return NUFFT_OK;
+}
+
+}  // namespace nufft

@@ -1,0 +1,352 @@
+"""``NUFFT``: the GB300 drop-in for the reference class ``pynufft.NUFFT``.
+
+Surface follows nufft/__init__.py:496-738 of the reference (pynufft 2025.2.1):
+``plan(om, Nd, Kd, Jd[, ft_axes][, batch])`` returns 0, ``forward``,
+``adjoint``, ``selfadjoint``, ``solve(y, 'cg', maxiter=...)`` and the stage
+methods ``x2xx``, ``xx2k``, ``k2y``, ``y2k``, ``k2xx``, ``xx2x``, ``k2y2k``,
+``xx2k_one2one``, ``k2xx_one2one``.  The ``batch`` argument follows the
+deprecated device class (linalg/nufft_hsa.py:152-242): x is Nd+(batch,),
+k is Kd+(batch,), y is (M, batch), coils share the points.
+
+Every transform runs on the GPU through the C ABI of libpynufft_gb300.so;
+there is no CPU path.  Inputs may be numpy arrays (results come back as
+numpy complex64), CUDA torch tensors (results stay on the device, no host
+synchronisation) or CPU torch tensors (copied in and out; pinned memory makes
+both copies asynchronous).  The reference's CPU path returns complex128 from
+``forward``/``k2y``/``y2k``; this one returns complex64 everywhere.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import c_int, c_int64, c_void_p
+
+import numpy
+
+from . import _lib
+from .plan_params import alpha_fit
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class NUFFT:
+    """Min-max NUFFT on one GB300 (see the module docstring)."""
+
+    def __init__(self, device_indx=None, legacy=None):
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise RuntimeError('pynufft_gb300 needs a CUDA device; it has no CPU fallback')
+        if device_indx is None:
+            dev = torch.device('cuda', torch.cuda.current_device())
+        elif isinstance(device_indx, int):
+            dev = torch.device('cuda', device_indx)
+        elif isinstance(device_indx, (str, torch.device)):
+            dev = torch.device(device_indx)
+        else:
+            # a device description from the reference's helper.device_list():
+            # the operator always runs on the current CUDA device
+            dev = torch.device('cuda', torch.cuda.current_device())
+        self.device = dev
+        self.dtype = numpy.complex64
+        self.processor = 'gb300'
+        self.debug = 0
+        self.Nd = ()
+        self.Kd = ()
+        self.Jd = ()
+        self.ndims = 0
+        self.ft_axes = ()
+        self.batch = None
+        self.ninst = 1
+        self._plan = None
+        self._lib = _lib.load()
+
+    # ------------------------------------------------------------------ plan
+    def plan(self, om, Nd, Kd, Jd, ft_axes=None, batch=None, deterministic=False,
+             bins=None, max_sub_points=None):
+        """Plan for the points ``om`` (M x ndim radians).
+
+        Argument checks follow helper.plan (src/_helper/helper.py:644-654):
+        ``TypeError`` when Nd/Kd/Jd are not tuples, ``KeyError`` when their
+        lengths differ.  ``deterministic=True`` selects the bitwise-reproducible
+        gridding mode.  ``bins``/``max_sub_points`` override the gridding bin
+        shape (see ``pynufft_gb300.autotune``).  Returns 0.
+        """
+        self._check_shapes(Nd, Kd, Jd)
+        ndim = len(Nd)
+        if ft_axes is not None and tuple(sorted(ft_axes)) != tuple(range(ndim)):
+            raise NotImplementedError('pynufft_gb300 transforms over all axes (ft_axes=None)')
+        B = 1 if batch is None else int(batch)
+        if B < 1:
+            raise ValueError('batch must be a positive integer')
+        return self._plan_common([om], Nd, Kd, Jd, batch, B, 1, deterministic, bins,
+                                 max_sub_points)
+
+    def plan_many(self, om_list, Nd, Kd, Jd, batch=None, deterministic=False, bins=None,
+                  max_sub_points=None):
+        """Plan ``len(om_list)`` independent instances that share Nd/Kd/Jd but
+        have their own points (uneven M).  Every transform then runs all
+        instances in the same kernel launches: x is (ninst,)+Nd[+(batch,)],
+        k is (ninst,)+Kd[+(batch,)] and y concatenates the instances' samples
+        in order.  Returns 0."""
+        self._check_shapes(Nd, Kd, Jd)
+        if len(om_list) < 1:
+            raise ValueError('om_list is empty')
+        B = 1 if batch is None else int(batch)
+        return self._plan_common(list(om_list), Nd, Kd, Jd, batch, B, len(om_list),
+                                 deterministic, bins, max_sub_points)
+
+    @staticmethod
+    def _check_shapes(Nd, Kd, Jd):
+        if type(Nd) != tuple:
+            raise TypeError('Nd must be tuple, e.g. (256, 256)')
+        if type(Kd) != tuple:
+            raise TypeError('Kd must be tuple, e.g. (512, 512)')
+        if type(Jd) != tuple:
+            raise TypeError('Jd must be tuple, e.g. (6, 6)')
+        if len(Nd) != len(Kd) or len(Nd) != len(Jd):
+            raise KeyError('Nd, Kd, Jd must be in the same length, e.g. '
+                           'Nd=(256,256),Kd=(512,512),Jd=(6,6)')
+
+    def _plan_common(self, oms, Nd, Kd, Jd, batch, B, ninst, deterministic, bins, max_sub):
+        torch = _torch()
+        self.release()
+        ndim = len(Nd)
+        flags = _lib.NUFFT_FLAG_DETERMINISTIC if deterministic else 0
+        h = c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.nufft_plan_create(ndim, _lib.int_array(Nd), _lib.int_array(Kd),
+                                                   _lib.int_array(Jd), B, ninst, flags,
+                                                   ctypes.byref(h)), 'plan')
+            self._plan = h
+            self._alpha = []
+            for d in range(ndim):
+                a, L = alpha_fit(int(Nd[d]), int(Jd[d]), int(Kd[d]))
+                self._alpha.append((a, L))
+                buf = (ctypes.c_float * 16)(*([float(v) for v in a] + [0.0] * (16 - a.size)))
+                _lib.check(self._lib.nufft_plan_set_alpha(h, d, buf, int(L)), 'plan')
+            if bins is not None or max_sub is not None:
+                bs = _lib.int_array(bins) if bins is not None else None
+                _lib.check(self._lib.nufft_plan_set_bins(h, bs, int(max_sub or 0)), 'plan')
+            counts = []
+            parts = []
+            on_dev = False
+            for om in oms:
+                om_t = self._om_tensor(om, ndim)
+                counts.append(om_t.shape[0])
+                parts.append(om_t)
+            if any(p.is_cuda for p in parts):
+                om_all = torch.cat([p.to(self.device) for p in parts]).contiguous()
+                on_dev = True
+                ptr = om_all.data_ptr()
+            else:
+                om_all = numpy.ascontiguousarray(numpy.concatenate([p.numpy() for p in parts]))
+                ptr = om_all.ctypes.data
+            cnt = (c_int64 * ninst)(*counts)
+            _lib.check(self._lib.nufft_set_points(h, cnt, c_void_p(ptr), 1 if on_dev else 0,
+                                                  self._stream()), 'plan')
+        self.Nd, self.Kd, self.Jd = tuple(Nd), tuple(Kd), tuple(Jd)
+        self.ndims = ndim
+        self.ft_axes = tuple(range(ndim))
+        self.batch = batch
+        self.B = B
+        self.ninst = ninst
+        self.counts = tuple(int(c) for c in counts)
+        self.M = (int(sum(counts)),)
+        self.deterministic = bool(deterministic)
+        self.Kdprod = int(numpy.prod(Kd))
+        self.Jdprod = int(numpy.prod(Jd))
+        self.st = {'M': numpy.int32(sum(counts)), 'Nd': self.Nd, 'Kd': self.Kd, 'Jd': self.Jd}
+        self.sn = self._host_sn()
+        return 0
+
+    def _om_tensor(self, om, ndim):
+        torch = _torch()
+        if isinstance(om, torch.Tensor):
+            t = om.detach().to(torch.float64)
+        else:
+            t = torch.from_numpy(numpy.ascontiguousarray(numpy.asarray(om, dtype=numpy.float64)))
+        if t.dim() == 1 and ndim == 1:
+            t = t.reshape(-1, 1)
+        if t.dim() != 2 or t.shape[1] != ndim:
+            raise ValueError(f'om must be (M, {ndim}), got {tuple(t.shape)}')
+        return t.contiguous()
+
+    def _host_sn(self):
+        """The Kronecker product of the per-axis scaling factors (Nd, complex64),
+        as the reference's ``sn`` attribute (nufft/_nufft_class_methods_cpu.py:84)."""
+        sn = numpy.ones(())
+        for d in range(self.ndims):
+            N, J, K = self.Nd[d], self.Jd[d], self.Kd[d]
+            al, Lin = self._alpha[d]
+            ain = (ctypes.c_float * 16)(*([float(v) for v in al] + [0.0] * (16 - al.size)))
+            a = (ctypes.c_float * 16)()
+            L = c_int()
+            snd = (ctypes.c_double * N)()
+            T = (ctypes.c_double * (J * J))()
+            _lib.check(self._lib.nufft_axis_params(N, J, K, ain, int(Lin), a, ctypes.byref(L),
+                                                   snd, T), 'sn')
+            shp = [1] * self.ndims
+            shp[d] = N
+            sn = sn * numpy.frombuffer(snd, dtype=numpy.float64).reshape(shp)
+        return numpy.asarray(sn.astype(numpy.complex64), order='C')
+
+    def release(self):
+        """Free the plan's device memory (nufft/_nufft_class_methods_device.py:653-683)."""
+        if getattr(self, '_plan', None) is not None:
+            self._lib.nufft_plan_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    def info(self):
+        m, ns, by = c_int64(), c_int64(), c_int64()
+        _lib.check(self._lib.nufft_plan_info(self._plan, ctypes.byref(m), ctypes.byref(ns),
+                                             ctypes.byref(by)), 'info')
+        return {'M': m.value, 'subproblems': ns.value, 'device_bytes': by.value}
+
+    # ------------------------------------------------------------- plumbing
+    def _stream(self):
+        torch = _torch()
+        return c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def _shape(self, kind):
+        lead = (self.ninst,) if self.ninst > 1 else ()
+        tail = (self.batch,) if self.batch is not None else ()
+        if kind == 'x':
+            return lead + self.Nd + tail
+        if kind == 'k':
+            return lead + self.Kd + tail
+        return self.M + tail
+
+    def _in(self, a, kind):
+        """-> (device complex64 tensor, how to return the result)."""
+        torch = _torch()
+        if self._plan is None:
+            raise RuntimeError('plan() has not been called')
+        shape = self._shape(kind)
+        if isinstance(a, torch.Tensor):
+            if tuple(a.shape) != shape:
+                raise ValueError(f'expected shape {shape}, got {tuple(a.shape)}')
+            if a.is_cuda:
+                return a.to(self.device, torch.complex64).contiguous(), ('cuda', None)
+            t = a.to(torch.complex64)
+            pinned = t.is_pinned()
+            d = t.to(self.device, non_blocking=pinned).contiguous()
+            return d, ('cpu', pinned)
+        arr = numpy.asarray(a)
+        if arr.shape != shape:
+            raise ValueError(f'expected shape {shape}, got {arr.shape}')
+        arr = numpy.ascontiguousarray(arr, dtype=numpy.complex64)
+        return torch.from_numpy(arr).to(self.device), ('numpy', None)
+
+    def _out(self, t, how):
+        torch = _torch()
+        kind, pinned = how
+        if kind == 'cuda':
+            return t
+        if kind == 'cpu':
+            if pinned:
+                o = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+                o.copy_(t, non_blocking=True)
+                torch.cuda.current_stream(self.device).synchronize()
+                return o
+            return t.cpu()
+        return t.cpu().numpy()
+
+    def _empty(self, kind):
+        torch = _torch()
+        return torch.empty(self._shape(kind), dtype=torch.complex64, device=self.device)
+
+    def _call(self, fn, a, kin, kout, name):
+        torch = _torch()
+        d, how = self._in(a, kin)
+        out = self._empty(kout)
+        with torch.cuda.device(self.device):
+            _lib.check(fn(self._plan, c_void_p(d.data_ptr()), c_void_p(out.data_ptr()),
+                          self._stream()), name)
+        return self._out(out, how)
+
+    # ------------------------------------------------------------ operators
+    def forward(self, x):
+        """y = k2y(xx2k(x2xx(x)))  (nufft/_nufft_class_methods_cpu.py:168-179)."""
+        return self._call(self._lib.nufft_forward, x, 'x', 'y', 'forward')
+
+    def adjoint(self, y):
+        """x = xx2x(k2xx(y2k(y))), scaled by 1/prod(Kd) (:181-193)."""
+        return self._call(self._lib.nufft_adjoint, y, 'y', 'x', 'adjoint')
+
+    def selfadjoint(self, x):
+        """adjoint(forward(x)) (:201-214)."""
+        return self._call(self._lib.nufft_selfadjoint, x, 'x', 'x', 'selfadjoint')
+
+    def x2xx(self, x):
+        return self._call(self._lib.nufft_x2xx, x, 'x', 'x', 'x2xx')
+
+    def xx2x(self, xx):
+        return self._call(self._lib.nufft_xx2x, xx, 'x', 'x', 'xx2x')
+
+    def xx2k(self, xx):
+        return self._call(self._lib.nufft_xx2k, xx, 'x', 'k', 'xx2k')
+
+    def k2xx(self, k):
+        return self._call(self._lib.nufft_k2xx, k, 'k', 'x', 'k2xx')
+
+    def k2y(self, k):
+        return self._call(self._lib.nufft_k2y, k, 'k', 'y', 'k2y')
+
+    def y2k(self, y):
+        return self._call(self._lib.nufft_y2k, y, 'y', 'k', 'y2k')
+
+    def k2y2k(self, k):
+        return self._call(self._lib.nufft_k2y2k, k, 'k', 'k', 'k2y2k')
+
+    # the reference's *_one2one variants are the single-coil stages
+    xx2k_one2one = xx2k
+    k2xx_one2one = k2xx
+
+    def forward_dom(self, x):
+        """d y / d om: an (ndim, M[, batch]) array with
+        dy[d, m] = sum_n x_n (-i (n_d - N_d/2)) exp(-i om_m . (n - N/2)),
+        computed as the NUFFT of (-i (n_d - N_d/2)) x."""
+        torch = _torch()
+        d, how = self._in(x, 'x')
+        out = torch.empty((self.ndims,) + self._shape('y'), dtype=torch.complex64,
+                          device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.nufft_forward_dom(self._plan, c_void_p(d.data_ptr()),
+                                                   c_void_p(out.data_ptr()), self._stream()),
+                       'forward_dom')
+        return self._out(out, how)
+
+    def solve(self, y, solver=None, *args, maxiter=None, rtol=1e-5, atol=0.0,
+              return_info=False, **kwargs):
+        """solve(y, 'cg', maxiter=...) (linalg/solve_cpu.py:256-288 via
+        nufft/_nufft_class_methods_cpu.py:150-166): CG on the k-space normal
+        operator, x0 = 0, scipy's rtol/atol stopping rule, then k2xx(k)/sn.
+        Other reference solvers are listed in ``pynufft_gb300.solvers``."""
+        if solver is None:
+            raise ValueError('solver must be given, e.g. solve(y, "cg", maxiter=20)')
+        if solver != 'cg':
+            from . import solvers
+            return solvers.solve(self, y, solver, *args, maxiter=maxiter, **kwargs)
+        if kwargs.get('tol') is not None:
+            rtol = kwargs.pop('tol')
+        torch = _torch()
+        d, how = self._in(y, 'y')
+        out = self._empty('x')
+        it = c_int(0)
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.nufft_solve_cg(self._plan, c_void_p(d.data_ptr()),
+                                                c_void_p(out.data_ptr()),
+                                                -1 if maxiter is None else int(maxiter),
+                                                float(rtol), float(atol),
+                                                ctypes.byref(it) if return_info else None,
+                                                self._stream()), 'solve')
+        x = self._out(out, how)
+        return (x, it.value) if return_info else x
