@@ -232,13 +232,19 @@ class OracleNUFFT:
     def _matvec(self, A, v):
         if self.threads <= 1:
             return A.dot(v)
+        if self._row_chunks is None:
+            self._row_chunks = {}
+        key = id(A)
+        if key not in self._row_chunks:
+            self._row_chunks[key] = [(a, b, A[a:b]) for a, b in self._chunks(A.shape[0])]
+        parts = self._row_chunks[key]
         out = np.empty(A.shape[0], dtype=np.result_type(A.dtype, v.dtype))
-        chunks = self._chunks(A.shape[0])
-        with ThreadPoolExecutor(len(chunks)) as ex:
-            def work(ab):
-                a, b = ab
-                out[a:b] = A[a:b].dot(v)
-            list(ex.map(work, chunks))
+
+        def work(p):
+            a, b, sub = p
+            out[a:b] = sub.dot(v)
+        with ThreadPoolExecutor(len(parts)) as ex:
+            list(ex.map(work, parts))
         return out
 
     def _fftn(self, a, inverse=False):

@@ -38,7 +38,7 @@ def test_stages_match_reference(NUFFT, case):
     Nd, Kd, Jd = _tup(g['Nd']), _tup(g['Kd']), _tup(g['Jd'])
     A = NUFFT(0)
     assert A.plan(g['om'], Nd, Kd, Jd) == 0
-    np.testing.assert_array_equal(A.sn, g['sn'])
+    np.testing.assert_allclose(A.sn, g['sn'], rtol=3e-7)   # float32 sn, 1 ulp
     got = {
         'x2xx': A.x2xx(g['x']), 'xx2k': A.xx2k(g['x2xx']), 'k2y': A.k2y(g['k']),
         'y2k': A.y2k(g['y']), 'k2xx': A.k2xx(g['k']), 'xx2x': A.xx2x(g['x']),
