@@ -96,6 +96,21 @@ int nufft_plan_destroy(nufft_plan_t plan);
  * nufft_set_points.  Zero entries keep the default. */
 int nufft_plan_set_bins(nufft_plan_t plan, const int* bin_shape, int max_sub_points);
 
+/* Lane mappings of the interpolation (k2y) and gridding (y2k) kernels for
+ * plans with fewer than 8 coils (plans with 8 or more always split coils
+ * across lanes).  0 keeps the default (tile / z-team).  Used by the
+ * autotuner; results are identical up to float32 rounding order. */
+#define NUFFT_K2Y_COIL  0   /* (internal) lanes over coils                    */
+#define NUFFT_K2Y_ZTEAM 1   /* J lanes per point along the innermost axis     */
+#define NUFFT_K2Y_POINT 2   /* one thread per point                           */
+#define NUFFT_K2Y_TILE  3   /* bin footprint staged in shared memory + z-teams */
+#define NUFFT_Y2K_COIL  0   /* (internal) lanes over coils                    */
+#define NUFFT_Y2K_ZTEAM 1   /* J lanes per point along the innermost axis     */
+#define NUFFT_Y2K_POINT 2   /* one thread per point                           */
+#define NUFFT_Y2K_GLOBAL 3  /* z-teams adding floats straight into the grid
+                               (no shared tile; not in deterministic mode)    */
+int nufft_plan_set_methods(nufft_plan_t plan, int k2y_method, int y2k_method);
+
 /* Query plan geometry: total points, number of gridding sub-problems and
  * bytes of device memory the plan holds. */
 int nufft_plan_info(nufft_plan_t plan, int64_t* M_total, int64_t* n_subproblems,

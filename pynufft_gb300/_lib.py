@@ -23,6 +23,8 @@ NUFFT_ENOPOINTS = 6
 NUFFT_ECG_BREAKDOWN = 7
 NUFFT_EUNSUPPORTED = 8
 NUFFT_FLAG_DETERMINISTIC = 1
+NUFFT_K2Y_ZTEAM, NUFFT_K2Y_POINT, NUFFT_K2Y_TILE = 1, 2, 3
+NUFFT_Y2K_ZTEAM, NUFFT_Y2K_POINT, NUFFT_Y2K_GLOBAL = 1, 2, 3
 
 # every symbol the header declares, with (restype, argtypes)
 SIGNATURES = {
@@ -37,6 +39,7 @@ SIGNATURES = {
     'nufft_plan_destroy': (c_int, [c_void_p]),
     'nufft_plan_set_bins': (c_int, [c_void_p, POINTER(c_int), c_int]),
     'nufft_plan_info': (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]),
+    'nufft_plan_set_methods': (c_int, [c_void_p, c_int, c_int]),
     'nufft_x2xx': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     'nufft_xx2k': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     'nufft_k2y': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -44,8 +44,14 @@ nufft::Geom nufft_plan_s::geom() const {
         g.coef[d] = (d < ndim) ? c : nullptr;
         if (d < ndim && c) c += (size_t)Ma * g.JP[d];
     }
+    g.wpt = d_wpt;
     g.sub = d_sub;
     g.nsub = nsub;
+    // lane mappings: coil-teams for B >= 8; otherwise the plan's choice, with
+    // the shared-memory tile gather and z-team gridding as defaults
+    g.kmethod = (B >= 8) ? NUFFT_K2Y_COIL : (k2y_method ? k2y_method : NUFFT_K2Y_TILE);
+    g.ymethod = (B >= 8) ? NUFFT_Y2K_COIL : (y2k_method ? y2k_method : NUFFT_Y2K_ZTEAM);
+    if ((flags & NUFFT_FLAG_DETERMINISTIC) && g.ymethod == NUFFT_Y2K_GLOBAL) g.ymethod = NUFFT_Y2K_ZTEAM;
     return g;
 }
 
@@ -219,6 +225,19 @@ int nufft_plan_set_bins(nufft_plan_t p, const int* bin_shape, int max_sub_points
         return NUFFT_EINVAL;
     }
     p->user_maxsub = max_sub_points;
+    return NUFFT_OK;
+}
+
+int nufft_plan_set_methods(nufft_plan_t p, int k2y_method, int y2k_method) {
+    NUFFT_TRY(need_plan(p, "nufft_plan_set_methods"));
+    if (k2y_method < 0 || k2y_method > NUFFT_K2Y_TILE || y2k_method < 0 ||
+        y2k_method > NUFFT_Y2K_GLOBAL) {
+        set_error("nufft_plan_set_methods: unknown method");
+        return NUFFT_EINVAL;
+    }
+    p->k2y_method = k2y_method;
+    p->y2k_method = y2k_method;
+    free_cg(p);   // captured graphs hold the old kernels
     return NUFFT_OK;
 }
 

@@ -49,114 +49,161 @@ __device__ __forceinline__ float sn_of(const ImgGeom& g, const int (&n)[3]) {
     return v;
 }
 
-__global__ void scale_kernel(ImgGeom g, const float2* __restrict__ in, float2* __restrict__ out) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.n_img;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        int64_t c = (e / g.B) % g.prodN;
-        int n[3] = {0, 0, 0};
-        for (int d = g.ndim - 1; d >= 0; --d) {
-            n[d] = (int)(c % g.N[d]);
-            c /= g.N[d];
-        }
-        const float s = sn_of(g, n);
-        const float2 v = in[e];
-        out[e] = make_float2(v.x * s, v.y * s);
+// Row-wise kernels: one block per row of the last axis (all other indices
+// fixed per block), threads along the row, so index arithmetic is one
+// division chain per block and the row's accesses are contiguous.
+__device__ __forceinline__ void row_index(const ImgGeom& g, int64_t r, const int* ext,
+                                          int64_t& inst, int (&n)[3]) {
+    // r enumerates (inst, i0[, i1]) over the extents ext of the leading axes
+    n[0] = n[1] = n[2] = 0;
+    for (int d = g.ndim - 2; d >= 0; --d) {
+        n[d] = (int)(r % ext[d]);
+        r /= ext[d];
     }
+    inst = r;
 }
 
-// grid[k] = x[k] * (sn[k] if apply_sn) * (-i (k_a - N_a/2) if dom_axis == a)
-// for k inside the Nd corner, 0 elsewhere.
-__global__ void pad_kernel(ImgGeom g, const float2* __restrict__ xx, float2* __restrict__ grid,
-                           int apply_sn, int dom_axis) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.n_grid;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int b = (int)(e % g.B);
-        int64_t c = e / g.B;
-        const int64_t inst = c / g.prodK;
-        c -= inst * g.prodK;
-        int n[3] = {0, 0, 0};
-        bool inside = true;
-        int64_t ni = 0, stride = 1;
-        for (int d = g.ndim - 1; d >= 0; --d) {
-            n[d] = (int)(c % g.K[d]);
-            c /= g.K[d];
-            inside = inside && (n[d] < g.N[d]);
-            ni += (int64_t)n[d] * stride;
-            stride *= g.N[d];
-        }
+__global__ void scale_rows_kernel(ImgGeom g, const float2* __restrict__ in, float2* __restrict__ out,
+                                  int64_t rows) {
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    int64_t inst;
+    int n[3];
+    row_index(g, r, g.N, inst, n);
+    const int L = g.N[g.ndim - 1];
+    const int B = g.B;
+    float s_lead = 1.f;
+    for (int d = 0; d < g.ndim - 1; ++d) s_lead *= __ldg(g.sn[d] + n[d]);
+    const float* snl = g.sn[g.ndim - 1];
+    const size_t base = (size_t)r * L * B;
+    for (int e = threadIdx.x; e < L * B; e += blockDim.x) {
+        const int k = (B == 1) ? e : e / B;
+        const float sc = s_lead * __ldg(snl + k);
+        const float2 v = __ldg(in + base + e);
+        out[base + e] = make_float2(v.x * sc, v.y * sc);
+    }
+  }
+}
+
+// grid row = x row * (sn if apply_sn) * (-i (n_a - N_a/2) if dom_axis == a),
+// zero outside the Nd corner
+__global__ void pad_rows_kernel(ImgGeom g, const float2* __restrict__ xx, float2* __restrict__ grid,
+                                int apply_sn, int dom_axis, int64_t rows) {
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    int64_t inst;
+    int n[3];
+    row_index(g, r, g.K, inst, n);
+    bool inside = true;
+    for (int d = 0; d < g.ndim - 1; ++d) inside = inside && (n[d] < g.N[d]);
+    const int last = g.ndim - 1;
+    const int KL = g.K[last], NL = g.N[last];
+    const int B = g.B;
+    float2* dst = grid + (size_t)r * KL * B;
+    if (!inside) {
+        for (int e = threadIdx.x; e < KL * B; e += blockDim.x) dst[e] = make_float2(0.f, 0.f);
+        continue;
+    }
+    float s_lead = 1.f;
+    if (apply_sn)
+        for (int d = 0; d < last; ++d) s_lead *= __ldg(g.sn[d] + n[d]);
+    float a_lead = 0.f;
+    if (dom_axis >= 0 && dom_axis < last) a_lead = (float)n[dom_axis] - 0.5f * (float)g.N[dom_axis];
+    int64_t xrow = inst;
+    for (int d = 0; d < last; ++d) xrow = xrow * g.N[d] + n[d];
+    const float2* src = xx + (size_t)xrow * NL * B;
+    for (int e = threadIdx.x; e < KL * B; e += blockDim.x) {
+        const int k = (B == 1) ? e : e / B;
         float2 v = make_float2(0.f, 0.f);
-        if (inside) {
-            v = __ldg(xx + (inst * g.prodN + ni) * g.B + b);
+        if (k < NL) {
+            v = __ldg(src + e);
             if (apply_sn) {
-                const float s = sn_of(g, n);
-                v.x *= s;
-                v.y *= s;
+                const float sc = s_lead * __ldg(g.sn[last] + k);
+                v.x *= sc;
+                v.y *= sc;
             }
             if (dom_axis >= 0) {
-                const float a = (float)n[dom_axis] - 0.5f * (float)g.N[dom_axis];
+                const float a = (dom_axis == last) ? (float)k - 0.5f * (float)NL : a_lead;
                 v = make_float2(a * v.y, -a * v.x);
             }
         }
-        grid[e] = v;
+        dst[e] = v;
     }
+  }
 }
 
-// xx[n] = grid[n] / prod(Kd) * (sn[n] if apply_sn) / (sn[n] if divide_sn)
-__global__ void crop_kernel(ImgGeom g, const float2* __restrict__ grid, float2* __restrict__ xx,
-                            int apply_sn, int divide_sn, float norm) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.n_img;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int b = (int)(e % g.B);
-        int64_t c = e / g.B;
-        const int64_t inst = c / g.prodN;
-        c -= inst * g.prodN;
-        int n[3] = {0, 0, 0};
-        int64_t ki = 0, stride = 1;
-        for (int d = g.ndim - 1; d >= 0; --d) {
-            n[d] = (int)(c % g.N[d]);
-            c /= g.N[d];
-            ki += (int64_t)n[d] * stride;
-            stride *= g.K[d];
-        }
-        float2 v = __ldg(grid + (inst * g.prodK + ki) * g.B + b);
-        float s = norm;
-        if (apply_sn) s *= sn_of(g, n);
-        v.x *= s;
-        v.y *= s;
+// x row = grid row (first N of the last axis) / prod(Kd) * (sn if apply_sn) / (sn if divide_sn)
+__global__ void crop_rows_kernel(ImgGeom g, const float2* __restrict__ grid, float2* __restrict__ xx,
+                                 int apply_sn, int divide_sn, float norm, int64_t rows) {
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    int64_t inst;
+    int n[3];
+    row_index(g, r, g.N, inst, n);
+    const int last = g.ndim - 1;
+    const int KL = g.K[last], NL = g.N[last];
+    const int B = g.B;
+    float s_lead = 1.f;
+    for (int d = 0; d < last; ++d) s_lead *= __ldg(g.sn[d] + n[d]);
+    int64_t krow = inst;
+    for (int d = 0; d < last; ++d) krow = krow * g.K[d] + n[d];
+    const float2* src = grid + (size_t)krow * KL * B;
+    float2* dst = xx + (size_t)r * NL * B;
+    for (int e = threadIdx.x; e < NL * B; e += blockDim.x) {
+        const int k = (B == 1) ? e : e / B;
+        float2 v = __ldg(src + e);
+        float sc = norm;
+        const float snv = s_lead * __ldg(g.sn[last] + k);
+        if (apply_sn) sc *= snv;
+        v.x *= sc;
+        v.y *= sc;
         if (divide_sn) {
-            const float t = sn_of(g, n);
-            v.x /= t;
-            v.y /= t;
+            v.x /= snv;
+            v.y /= snv;
         }
-        xx[e] = v;
+        dst[e] = v;
     }
+  }
 }
 
-static int blocks_for(const nufft_plan_s* p, int64_t n) {
-    int64_t b = (n + 255) / 256;
-    return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)p->num_sms * 32));
+static int64_t rows_of(const ImgGeom& g, const int* ext, int ninst) {
+    int64_t r = ninst;
+    for (int d = 0; d < g.ndim - 1; ++d) r *= ext[d];
+    return r;
+}
+
+static unsigned row_blocks(const nufft_plan_s* p, int64_t rows) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(rows, (int64_t)p->num_sms * 8));
+}
+
+static int row_threads(int len) {
+    int t = 32;
+    while (t < len && t < 256) t <<= 1;
+    return t;
 }
 
 int launch_scale(const nufft_plan_s* p, const float2* in, float2* out, cudaStream_t s) {
     ImgGeom g = img_geom(p);
-    scale_kernel<<<blocks_for(p, g.n_img), 256, 0, s>>>(g, in, out);
-    return check_launch("scale_kernel");
+    const int64_t rows = rows_of(g, g.N, p->ninst);
+    scale_rows_kernel<<<row_blocks(p, rows), row_threads(g.N[g.ndim - 1] * g.B), 0, s>>>(g, in, out,
+                                                                                         rows);
+    return check_launch("scale_rows_kernel");
 }
 
 int launch_pad(const nufft_plan_s* p, const float2* xx, float2* grid, bool apply_sn,
                int dom_axis, cudaStream_t s) {
     ImgGeom g = img_geom(p);
-    pad_kernel<<<blocks_for(p, g.n_grid), 256, 0, s>>>(g, xx, grid, apply_sn ? 1 : 0, dom_axis);
-    return check_launch("pad_kernel");
+    const int64_t rows = rows_of(g, g.K, p->ninst);
+    pad_rows_kernel<<<row_blocks(p, rows), row_threads(g.K[g.ndim - 1] * g.B), 0, s>>>(
+        g, xx, grid, apply_sn ? 1 : 0, dom_axis, rows);
+    return check_launch("pad_rows_kernel");
 }
 
 int launch_crop(const nufft_plan_s* p, const float2* grid, float2* xx, bool apply_sn,
                 bool divide_sn, cudaStream_t s) {
     ImgGeom g = img_geom(p);
     const float norm = (float)(1.0 / (double)p->prodK);
-    crop_kernel<<<blocks_for(p, g.n_img), 256, 0, s>>>(g, grid, xx, apply_sn ? 1 : 0,
-                                                        divide_sn ? 1 : 0, norm);
-    return check_launch("crop_kernel");
+    const int64_t rows = rows_of(g, g.N, p->ninst);
+    crop_rows_kernel<<<row_blocks(p, rows), row_threads(g.N[g.ndim - 1] * g.B), 0, s>>>(
+        g, grid, xx, apply_sn ? 1 : 0, divide_sn ? 1 : 0, norm, rows);
+    return check_launch("crop_rows_kernel");
 }
 
 int fft_init(nufft_plan_s* p) {

@@ -1,7 +1,4 @@
-// Interpolation (k2y) and gridding (y2k) kernels, templated on the number of
-// dimensions DIM, the per-axis neighbour bound JM (compile-time loop length;
-// the runtime J[d] <= JM masks the tail) and the team width G (lanes that
-// share one point and split the coils between them).
+// Interpolation (k2y) and gridding (y2k) kernels.
 //
 //   k2y  y[m,b]  = sum_{j} prod_d coef_d[m,j_d] * k[idx(m,j), b]
 //                  (the CSR product sp . k of _k2y_cpu,
@@ -11,11 +8,28 @@
 // coef_d holds conj(u) exactly as the reference's CSR values
 // (helper.min_max returns u.T.conj(), src/_helper/helper.py:606-618).
 //
-// The sum over the Kronecker footprint is factorised axis by axis
-// (sum_i c0_i sum_j c1_j sum_k c2_k g_ijk), so a 3D point costs
-// J^3 + J^2 + J complex multiply-adds instead of 2 J^3.  The two innermost
-// axes are unrolled; the outermost axis loop stays rolled and re-reads its
-// coefficient through L1, which bounds code size for every JM.
+// Two lane mappings, chosen by the coil count B:
+//  * z-teams (B < 8): a team of J_z lanes (J of the innermost axis) shares one
+//    point, lane k owning footprint offset k along the innermost axis.  A
+//    team's grid accesses are J_z consecutive cells, so a warp touches ~2
+//    sectors per team instead of one scattered sector per lane; the sum over
+//    k is a shuffle reduction inside the team.  Coils loop inside the lane.
+//  * coil-teams (B >= 8): G = 8 or 32 lanes share one point and split the
+//    coils, so consecutive lanes touch consecutive coils of one cell.
+// Both factorise the footprint sum axis by axis (outer axis rolled, re-read
+// through L1; middle axis in registers; inner axis across lanes or unrolled).
+//
+// Gridding accumulates in shared memory with native integer atomics: this
+// GPU has no native shared-memory float add (a float atomicAdd there is a
+// compare-and-swap loop).  The fast mode converts each float contribution to
+// 32-bit fixed point with a power-of-two scale chosen per sub-problem from a
+// bound on any cell's sum (sum over the sub-problem's points of
+// W_p (|re y| + |im y|), W_p = prod_d max_j |coef|), so no cell can overflow
+// and the rounding unit stays below float32 resolution for sub-problems of a
+// few hundred points; the tile is converted back to float and added to the
+// grid with vector atomics.  The deterministic mode uses 64-bit fixed point
+// with one global scale and flushes integers, so the whole sum is exact and
+// order-independent.
 #pragma once
 #include "nufft_internal.cuh"
 
@@ -23,6 +37,9 @@ namespace nufft {
 
 __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // a * conj(b)
     return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 __device__ __forceinline__ void cfma(float2& acc, float2 a, float2 b) {  // acc += a*b
     acc.x = fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x));
@@ -38,6 +55,64 @@ __device__ __forceinline__ int inst_of_sorted(const int64_t* start, int ninst, i
     return lo;
 }
 
+__device__ __forceinline__ int wrap1(int q, int K) { return (q >= K) ? q - K : q; }
+__device__ __forceinline__ int wrapn(int q, int K) {
+    while (q >= K) q -= K;
+    return q;
+}
+
+// Walks the cells of a DIM-dimensional tile (extents T, row-major) with a
+// fixed stride, keeping the coordinates incrementally (one division chain
+// per thread instead of one per cell).
+template <int DIM>
+struct TileWalk {
+    int t[3], st[3], T[3];
+    __device__ __forceinline__ void init(const int* ext, int first, int stride) {
+        T[0] = ext[0]; T[1] = (DIM > 1) ? ext[1] : 1; T[2] = (DIM > 2) ? ext[2] : 1;
+        // the last tile axis is the fastest: index = (t0*T1 + t1)*T2 + t2 in 3D
+        t[0] = t[1] = t[2] = 0; st[0] = st[1] = st[2] = 0;
+        if (DIM == 1) { t[0] = first; st[0] = stride; return; }
+        const int Tl = T[DIM - 1];
+        int e = first, s = stride;
+        t[DIM - 1] = e % Tl; st[DIM - 1] = s % Tl;
+        e /= Tl; s /= Tl;
+        if (DIM == 3) { t[1] = e % T[1]; st[1] = s % T[1]; e /= T[1]; s /= T[1]; }
+        t[0] = e;
+        st[0] = s;
+    }
+    __device__ __forceinline__ void next() {
+        if (DIM == 1) { t[0] += st[0]; return; }
+        t[DIM - 1] += st[DIM - 1];
+        int carry = 0;
+        if (t[DIM - 1] >= T[DIM - 1]) { t[DIM - 1] -= T[DIM - 1]; carry = 1; }
+        if (DIM == 3) {
+            t[1] += st[1] + carry;
+            carry = 0;
+            if (t[1] >= T[1]) { t[1] -= T[1]; carry = 1; }
+        }
+        t[0] += st[0] + carry;
+    }
+    // flat grid cell (inside one instance) of tile coordinate t for origin o
+    __device__ __forceinline__ size_t cell(const Geom& g, const int (&o)[3]) const {
+        size_t gc = 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) gc = gc * g.K[d] + wrapn(o[d] + t[d], g.K[d]);
+        return gc;
+    }
+};
+
+// Tile origin of a sub-problem.
+template <int DIM>
+__device__ __forceinline__ void tile_origin(const Geom& g, const int4& sp, int (&o)[3]) {
+    int64_t lb = sp.x - (int64_t)sp.w * g.nbin_inst;
+    o[0] = o[1] = o[2] = 0;
+#pragma unroll
+    for (int d = DIM - 1; d >= 0; --d) {
+        o[d] = (int)(lb % g.nb[d]) * g.bs[d];
+        lb /= g.nb[d];
+    }
+}
+
 // Load one point's wrapped footprint indices and coefficients for axis d.
 template <int JM>
 __device__ __forceinline__ void load_axis(const Geom& g, int d, int64_t s, int (&idx)[JM],
@@ -48,8 +123,7 @@ __device__ __forceinline__ void load_axis(const Geom& g, int d, int64_t s, int (
 #pragma unroll
     for (int j = 0; j < JM; ++j) {
         if (j < J) {
-            int q = p + j;
-            idx[j] = (q >= K) ? q - K : q;
+            idx[j] = wrap1(p + j, K);
             c[j] = __ldg(src + j);
         } else {
             idx[j] = 0;
@@ -58,9 +132,82 @@ __device__ __forceinline__ void load_axis(const Geom& g, int d, int64_t s, int (
     }
 }
 
+// Sum of v over the TS lanes of this lane's team (teams are TS-aligned);
+// the first lane of the team receives the total.
+__device__ __forceinline__ float2 team_sum(float2 v, int k, int TS) {
+#pragma unroll
+    for (int off = 1; off < 16; off <<= 1) {
+        const float ox = __shfl_down_sync(0xffffffffu, v.x, off);
+        const float oy = __shfl_down_sync(0xffffffffu, v.y, off);
+        if (off < TS && k + off < TS) {
+            v.x += ox;
+            v.y += oy;
+        }
+    }
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// k2y, z-teams (B < 8)
+// ---------------------------------------------------------------------------
+template <int DIM, int JM>
+__global__ void __launch_bounds__(256) k2y_zteam_kernel(Geom g, const float2* __restrict__ grid,
+                                                        float2* __restrict__ y) {
+    constexpr int DI = DIM - 1;
+    constexpr int DY = (DIM > 1) ? DIM - 2 : 0;
+    const int TS = g.J[DI];
+    const int NT = 32 / TS;
+    const int lane = threadIdx.x & 31;
+    const int team = lane / TS, k = lane - team * TS;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t s = warp * NT + team;
+    const bool active = (team < NT) && (s < g.M);
+    const int64_t sl = active ? s : 0;
+    const int B = g.B;
+    const int inst = (g.ninst > 1) ? inst_of_sorted(g.inst_start, g.ninst, sl) : 0;
+    const float2* __restrict__ base = grid + (size_t)inst * g.prodK * B;
+
+    const int pz = __ldg(g.pos[DI] + sl);
+    const int iz = wrap1(pz + k, g.K[DI]);
+    const float2 cz = __ldg(g.coef[DI] + sl * g.JP[DI] + k);
+    int iy[JM];
+    float2 cy[JM];
+    if constexpr (DIM > 1) load_axis<JM>(g, DY, sl, iy, cy);
+    const int Kz = g.K[DI], Ky = g.K[DY];
+    const int p0 = __ldg(g.pos[0] + sl), K0 = g.K[0], J0 = g.J[0];
+    const float2* c0src = g.coef[0] + sl * g.JP[0];
+
+    for (int b = 0; b < B; ++b) {
+        float2 acc = make_float2(0.f, 0.f);
+        if constexpr (DIM == 1) {
+            acc = __ldg(base + (size_t)iz * B + b);
+        } else if constexpr (DIM == 2) {
+#pragma unroll
+            for (int j = 0; j < JM; ++j)
+                cfma(acc, cy[j], __ldg(base + ((size_t)iy[j] * Kz + iz) * B + b));
+        } else {
+#pragma unroll 1
+            for (int i = 0; i < J0; ++i) {
+                const size_t plane = (size_t)wrap1(p0 + i, K0) * Ky;
+                float2 t = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int j = 0; j < JM; ++j)
+                    cfma(t, cy[j], __ldg(base + ((plane + iy[j]) * Kz + iz) * B + b));
+                cfma(acc, __ldg(c0src + i), t);
+            }
+        }
+        acc = cmul(acc, cz);
+        acc = team_sum(acc, k, TS);
+        if (active && k == 0) y[(size_t)__ldg(g.perm + s) * B + b] = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k2y, coil-teams (B >= 8)
+// ---------------------------------------------------------------------------
 template <int DIM, int JM, int G>
-__global__ void __launch_bounds__(256) k2y_kernel(Geom g, const float2* __restrict__ grid,
-                                                  float2* __restrict__ y) {
+__global__ void __launch_bounds__(256) k2y_coil_kernel(Geom g, const float2* __restrict__ grid,
+                                                       float2* __restrict__ y) {
     const int64_t team = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / G;
     const int lane = threadIdx.x % G;
     if (team >= g.M) return;
@@ -70,9 +217,8 @@ __global__ void __launch_bounds__(256) k2y_kernel(Geom g, const float2* __restri
     const int B = g.B;
     const float2* __restrict__ base = grid + (size_t)inst * g.prodK * B;
 
-    // innermost (fastest) axis and the one above it live in registers
-    constexpr int DI = DIM - 1;                    // innermost axis
-    constexpr int DY = (DIM > 1) ? DIM - 2 : 0;    // the axis above it
+    constexpr int DI = DIM - 1;
+    constexpr int DY = (DIM > 1) ? DIM - 2 : 0;
     int iz[JM], iy[JM];
     float2 cz[JM], cy[JM];
     load_axis<JM>(g, DI, s, iz, cz);
@@ -99,9 +245,7 @@ __global__ void __launch_bounds__(256) k2y_kernel(Geom g, const float2* __restri
         } else {
 #pragma unroll 1
             for (int i = 0; i < J0; ++i) {
-                int q = p0 + i;
-                if (q >= K0) q -= K0;
-                const size_t plane = (size_t)q * Ky;
+                const size_t plane = (size_t)wrap1(p0 + i, K0) * Ky;
                 float2 ti = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int j = 0; j < JM; ++j) {
@@ -118,45 +262,160 @@ __global__ void __launch_bounds__(256) k2y_kernel(Geom g, const float2* __restri
     }
 }
 
-// Fixed-point conversion of one contribution for the deterministic mode.
-__device__ __forceinline__ unsigned long long to_fixed(float v, float scale) {
-    return (unsigned long long)__float2ll_rn(v * scale);
-}
-
-template <bool DET>
-__device__ __forceinline__ void smem_add(unsigned char* smem_raw, int e, float2 w, float scale) {
-    if (DET) {
-        unsigned long long* sm = reinterpret_cast<unsigned long long*>(smem_raw);
-        atomicAdd(sm + 2 * e, to_fixed(w.x, scale));
-        atomicAdd(sm + 2 * e + 1, to_fixed(w.y, scale));
-    } else {
-        float* sm = reinterpret_cast<float*>(smem_raw);
-        atomicAdd(sm + 2 * e, w.x);
-        atomicAdd(sm + 2 * e + 1, w.y);
-    }
-}
-
-// One thread block per gridding sub-problem (a bin, or a chunk of a crowded
-// bin).  The block accumulates its points into a shared-memory tile covering
-// the bin plus the J-1 halo, then adds the tile to the global grid with
-// vector atomics.  DET selects exact 64-bit fixed-point accumulation
-// (integer adds are associative, so the result does not depend on the order
-// in which threads or blocks arrive).
-template <int DIM, int JM, int G, bool DET>
-__global__ void __launch_bounds__(256) y2k_kernel(Geom g, const float2* __restrict__ y,
-                                                  float2* __restrict__ grid,
-                                                  unsigned long long* __restrict__ igrid,
-                                                  int bc, const double* __restrict__ dscal) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int4 sp = g.sub[blockIdx.x];
-    const int inst = sp.w;
-    int64_t lb = sp.x - (int64_t)inst * g.nbin_inst;
-    int o[3] = {0, 0, 0};
+// ---------------------------------------------------------------------------
+// k2y, one thread per point, single coil: each footprint row along the
+// innermost axis is read with 16-byte loads (3 loads instead of 6 for J = 6
+// on an even start), halving the L1 requests of the scattered gather.
+// Rows that wrap around the grid edge, or an odd innermost extent, fall
+// back to 8-byte loads.
+// ---------------------------------------------------------------------------
+template <int JM>
+__device__ __forceinline__ float2 row_dot(const float2* __restrict__ row, int pz, int Jz, int Kz,
+                                          bool vec_ok, const float2 (&cz)[JM]) {
+    float2 t = make_float2(0.f, 0.f);
+    const int odd = pz & 1;
+    const int pa = pz - odd;
+    constexpr int NV = (JM + 2) / 2;
+    const int nv = (odd + Jz + 1) >> 1;
+    if (vec_ok && pa + 2 * nv <= Kz) {
+        const float4* r4 = reinterpret_cast<const float4*>(row + pa);
+        float4 v[NV];
 #pragma unroll
-    for (int d = DIM - 1; d >= 0; --d) {
-        o[d] = (int)(lb % g.nb[d]) * g.bs[d];
-        lb /= g.nb[d];
+        for (int q = 0; q < NV; ++q) v[q] = (q < nv) ? __ldg(r4 + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (odd) {
+#pragma unroll
+            for (int k = 0; k < JM; ++k) {
+                const float4 q = v[(k + 1) >> 1];
+                const float2 c = ((k + 1) & 1) ? make_float2(q.z, q.w) : make_float2(q.x, q.y);
+                cfma(t, cz[k], c);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < JM; ++k) {
+                const float4 q = v[k >> 1];
+                const float2 c = (k & 1) ? make_float2(q.z, q.w) : make_float2(q.x, q.y);
+                cfma(t, cz[k], c);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < JM; ++k)
+            if (k < Jz) cfma(t, cz[k], __ldg(row + wrap1(pz + k, Kz)));
     }
+    return t;
+}
+
+template <int DIM, int JM>
+__global__ void __launch_bounds__(256) k2y_point_kernel(Geom g, const float2* __restrict__ grid,
+                                                        float2* __restrict__ y) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= g.M) return;
+    const int inst = (g.ninst > 1) ? inst_of_sorted(g.inst_start, g.ninst, s) : 0;
+    const float2* __restrict__ base = grid + (size_t)inst * g.prodK;
+    constexpr int DI = DIM - 1;
+    constexpr int DY = (DIM > 1) ? DIM - 2 : 0;
+    const int Kz = g.K[DI], Jz = g.J[DI];
+    const bool vec_ok = ((Kz & 1) == 0) && ((reinterpret_cast<uintptr_t>(base) & 15) == 0);
+    const int pz = __ldg(g.pos[DI] + s);
+    float2 cz[JM];
+    {
+        const float2* src = g.coef[DI] + s * g.JP[DI];
+#pragma unroll
+        for (int k = 0; k < JM; ++k) cz[k] = (k < Jz) ? __ldg(src + k) : make_float2(0.f, 0.f);
+    }
+    float2 acc = make_float2(0.f, 0.f);
+    if constexpr (DIM == 1) {
+        acc = row_dot<JM>(base, pz, Jz, Kz, vec_ok, cz);
+    } else {
+        int iy[JM];
+        float2 cy[JM];
+        load_axis<JM>(g, DY, s, iy, cy);
+        const int Jy = g.J[DY];
+        if constexpr (DIM == 2) {
+#pragma unroll
+            for (int j = 0; j < JM; ++j)
+                if (j < Jy) cfma(acc, cy[j], row_dot<JM>(base + (size_t)iy[j] * Kz, pz, Jz, Kz, vec_ok, cz));
+        } else {
+            const int p0 = __ldg(g.pos[0] + s), K0 = g.K[0], J0 = g.J[0], Ky = g.K[DY];
+            const float2* c0src = g.coef[0] + s * g.JP[0];
+#pragma unroll 1
+            for (int i = 0; i < J0; ++i) {
+                const size_t plane = (size_t)wrap1(p0 + i, K0) * Ky;
+                float2 t = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int j = 0; j < JM; ++j)
+                    if (j < Jy)
+                        cfma(t, cy[j], row_dot<JM>(base + (plane + iy[j]) * Kz, pz, Jz, Kz, vec_ok, cz));
+                cfma(acc, __ldg(c0src + i), t);
+            }
+        }
+    }
+    y[__ldg(g.perm + s)] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// y2k straight into the global grid (B < 8, fast mode only): z-teams add
+// float contributions with vector atomics performed in L2; no shared tile,
+// no flush, no fixed point.  Suited to sparse trajectories where a bin's
+// tile would hold few contributions per cell.
+// ---------------------------------------------------------------------------
+template <int DIM, int JM>
+__global__ void __launch_bounds__(256) y2k_global_kernel(Geom g, const float2* __restrict__ y,
+                                                         float2* __restrict__ grid) {
+    constexpr int DI = DIM - 1;
+    constexpr int DY = (DIM > 1) ? DIM - 2 : 0;
+    const int TS = g.J[DI];
+    const int NT = 32 / TS;
+    const int lane = threadIdx.x & 31;
+    const int team = lane / TS, k = lane - team * TS;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t s = warp * NT + team;
+    if (team >= NT || s >= g.M) return;
+    const int B = g.B;
+    const int inst = (g.ninst > 1) ? inst_of_sorted(g.inst_start, g.ninst, s) : 0;
+    float2* __restrict__ base = grid + (size_t)inst * g.prodK * B;
+    const int iz = wrap1(__ldg(g.pos[DI] + s) + k, g.K[DI]);
+    const float2 cz = __ldg(g.coef[DI] + s * g.JP[DI] + k);
+    int iy[JM];
+    float2 cy[JM];
+    if constexpr (DIM > 1) load_axis<JM>(g, DY, s, iy, cy);
+    const int Kz = g.K[DI], Ky = g.K[DY];
+    const int p0 = __ldg(g.pos[0] + s), K0 = g.K[0], J0 = g.J[0];
+    const float2* c0src = g.coef[0] + s * g.JP[0];
+    const int m = __ldg(g.perm + s);
+    for (int b = 0; b < B; ++b) {
+        const float2 v = cmulc(__ldg(y + (size_t)m * B + b), cz);
+        if constexpr (DIM == 1) {
+            atomicAdd(base + (size_t)iz * B + b, v);
+        } else {
+            const int ni = (DIM > 2) ? J0 : 1;
+#pragma unroll 1
+            for (int i = 0; i < ni; ++i) {
+                const float2 wi = (DIM > 2) ? cmulc(v, __ldg(c0src + i)) : v;
+                const size_t plane = (DIM > 2) ? (size_t)wrap1(p0 + i, K0) * Ky : 0;
+#pragma unroll
+                for (int j = 0; j < JM; ++j) {
+                    if (j >= g.J[DY]) continue;
+                    atomicAdd(base + ((plane + iy[j]) * Kz + iz) * B + b, cmulc(wi, cy[j]));
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k2y, shared-memory tile per sub-problem (B < 8): the block stages the
+// bin's footprint (bin + J-1 halo) in shared memory with coalesced row loads,
+// then z-teams gather from it; every point of a bin is served by one SM.
+// ---------------------------------------------------------------------------
+template <int DIM, int JM>
+__global__ void __launch_bounds__(256) k2y_tile_kernel(Geom g, const float2* __restrict__ grid,
+                                                       float2* __restrict__ y) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* tile = reinterpret_cast<float2*>(smem_raw);
+    const int4 sp = g.sub[blockIdx.x];
+    int o[3];
+    tile_origin<DIM>(g, sp, o);
     constexpr int DI = DIM - 1;
     constexpr int DY = (DIM > 1) ? DIM - 2 : 0;
     const int Tz = g.T[DI];
@@ -165,91 +424,308 @@ __global__ void __launch_bounds__(256) y2k_kernel(Geom g, const float2* __restri
 #pragma unroll
     for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
     const int B = g.B;
-    const float scale = DET ? (float)dscal[1] : 1.f;
-    const int team = threadIdx.x / G, lane = threadIdx.x % G, nteam = blockDim.x / G;
+    const int TS = g.J[DI], NT = 32 / TS;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int team = lane / TS, k = lane - team * TS;
     const int J0 = g.J[0];
+    const size_t ibase = (size_t)sp.w * g.prodK;
+    const int per_round = nwarps * NT;
+    const int end = sp.y + sp.z;
+
+    for (int b = 0; b < B; ++b) {
+        TileWalk<DIM> w;
+        w.init(g.T, threadIdx.x, blockDim.x);
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x, w.next())
+            tile[c] = __ldg(grid + (ibase + w.cell(g, o)) * B + b);
+        __syncthreads();
+        for (int base_s = sp.y; base_s < end; base_s += per_round) {
+            const int s = base_s + warp * NT + team;
+            const bool active = (team < NT) && (s < end);
+            const int sl = active ? s : sp.y;
+            const int lz = __ldg(g.pos[DI] + sl) - o[DI] + k;
+            const float2 cz = __ldg(g.coef[DI] + (size_t)sl * g.JP[DI] + k);
+            float2 acc = make_float2(0.f, 0.f);
+            if constexpr (DIM == 1) {
+                acc = tile[lz];
+            } else {
+                const int ly = __ldg(g.pos[DY] + sl) - o[DY];
+                float2 cy[JM];
+                const float2* src = g.coef[DY] + (size_t)sl * g.JP[DY];
+#pragma unroll
+                for (int j = 0; j < JM; ++j)
+                    cy[j] = (j < g.J[DY]) ? __ldg(src + j) : make_float2(0.f, 0.f);
+                if constexpr (DIM == 2) {
+#pragma unroll
+                    for (int j = 0; j < JM; ++j)
+                        if (j < g.J[DY]) cfma(acc, cy[j], tile[(ly + j) * Tz + lz]);
+                } else {
+                    const int lx = __ldg(g.pos[0] + sl) - o[0];
+                    const float2* c0src = g.coef[0] + (size_t)sl * g.JP[0];
+#pragma unroll 1
+                    for (int i = 0; i < J0; ++i) {
+                        const float2* row = tile + ((lx + i) * Ty + ly) * Tz + lz;
+                        float2 t = make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int j = 0; j < JM; ++j)
+                            if (j < g.J[DY]) cfma(t, cy[j], row[j * Tz]);
+                        cfma(acc, __ldg(c0src + i), t);
+                    }
+                }
+            }
+            acc = cmul(acc, cz);
+            acc = team_sum(acc, k, TS);
+            if (active && k == 0) y[(size_t)__ldg(g.perm + s) * B + b] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// y2k shared pieces
+// ---------------------------------------------------------------------------
+// Fixed-point accumulator types: 32-bit with a per-sub-problem scale (fast
+// mode) or 64-bit with a global scale (deterministic mode).
+template <bool DET> struct Acc;
+template <> struct Acc<false> {
+    using T = unsigned int;
+    static __device__ __forceinline__ T fix(float v, float s) { return (T)__float2int_rn(v * s); }
+};
+template <> struct Acc<true> {
+    using T = unsigned long long;
+    static __device__ __forceinline__ T fix(float v, float s) { return (T)__float2ll_rn(v * s); }
+};
+
+// Per-coil fixed-point scales of one sub-problem (fast mode), written to
+// scale[0..bcur).  Requires a block-wide barrier afterwards.
+__device__ __forceinline__ void subproblem_scales(const Geom& g, const int4& sp, const float2* y,
+                                                  int b0, int bcur, float* bound, float* scale) {
+    for (int b = threadIdx.x; b < bcur; b += blockDim.x) bound[b] = 0.f;
+    __syncthreads();
+    const int B = g.B;
+    for (int b = 0; b < bcur; ++b) {
+        float acc = 0.f;
+        for (int s = sp.y + threadIdx.x; s < sp.y + sp.z; s += blockDim.x) {
+            const float2 v = __ldg(y + (size_t)__ldg(g.perm + s) * B + b0 + b);
+            acc += __ldg(g.wpt + s) * (fabsf(v.x) + fabsf(v.y));
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        if ((threadIdx.x & 31) == 0 && acc > 0.f) atomicAdd(bound + b, acc);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < bcur; b += blockDim.x) {
+        // |sum of any cell| <= bound < 2^e, so a scale of 2^(30-e) keeps it < 2^30
+        int e = 0;
+        const float bb = bound[b] * 1.001f;
+        if (bb > 0.f && isfinite(bb)) frexpf(bb, &e);
+        scale[b] = ldexpf(1.f, 30 - e);
+    }
+    __syncthreads();
+}
+
+// Flush one accumulated tile chunk into the global grid (float, fast mode)
+// or the global fixed-point grid (deterministic mode).  Layout of the tile:
+// element e = cell * bcur + b (coil fastest) when CELL_MAJOR, else
+// b * ncell + cell; re plane first, im plane at offset nsm.
+template <int DIM, bool DET, bool CELL_MAJOR>
+__device__ __forceinline__ void flush_tile(const Geom& g, const int (&o)[3], int inst, int ncell,
+                                           int b0, int bcur, const typename Acc<DET>::T* tile,
+                                           const float* scale, float2* __restrict__ grid,
+                                           unsigned long long* __restrict__ igrid) {
+    const int nsm = ncell * bcur;
+    const size_t ibase = (size_t)inst * g.prodK;
+    const int B = g.B;
+    for (int b = 0; b < bcur; ++b) {
+        const float inv = DET ? 1.f : 1.f / scale[b];
+        TileWalk<DIM> w;
+        w.init(g.T, threadIdx.x, blockDim.x);
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x, w.next()) {
+            const int e = CELL_MAJOR ? c * bcur + b : b * ncell + c;
+            const typename Acc<DET>::T vx = tile[e], vy = tile[nsm + e];
+            if (vx == 0 && vy == 0) continue;
+            const size_t gi = (ibase + w.cell(g, o)) * B + b0 + b;
+            if constexpr (DET) {
+                if (vx) atomicAdd(igrid + 2 * gi, (unsigned long long)vx);
+                if (vy) atomicAdd(igrid + 2 * gi + 1, (unsigned long long)vy);
+            } else {
+                atomicAdd(grid + gi, make_float2(__int2float_rn((int)vx) * inv,
+                                                 __int2float_rn((int)vy) * inv));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// y2k, z-teams (B < 8): tile layout b-major (lanes of a team hit consecutive
+// words of one plane)
+// ---------------------------------------------------------------------------
+template <int DIM, int JM, bool DET>
+__global__ void __launch_bounds__(256) y2k_zteam_kernel(Geom g, const float2* __restrict__ y,
+                                                        float2* __restrict__ grid,
+                                                        unsigned long long* __restrict__ igrid,
+                                                        int bc, const double* __restrict__ dscal) {
+    using T = typename Acc<DET>::T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float s_bound[8], s_scale[8];
+    const int4 sp = g.sub[blockIdx.x];
+    const int inst = sp.w;
+    int o[3];
+    tile_origin<DIM>(g, sp, o);
+    constexpr int DI = DIM - 1;
+    constexpr int DY = (DIM > 1) ? DIM - 2 : 0;
+    const int Tz = g.T[DI];
+    const int Ty = (DIM > 1) ? g.T[DY] : 1;
+    int ncell = 1;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
+    const int B = g.B;
+    const int TS = g.J[DI], NT = 32 / TS;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int team = lane / TS, k = lane - team * TS;
+    const int J0 = g.J[0];
+    T* tile = reinterpret_cast<T*>(smem_raw);
 
     for (int b0 = 0; b0 < B; b0 += bc) {
         const int bcur = min(bc, B - b0);
         const int nsm = ncell * bcur;
-        if (DET) {
-            unsigned long long* sm = reinterpret_cast<unsigned long long*>(smem_raw);
-            for (int e = threadIdx.x; e < 2 * nsm; e += blockDim.x) sm[e] = 0ull;
+        for (int e = threadIdx.x; e < 2 * nsm; e += blockDim.x) tile[e] = 0;
+        if constexpr (DET) {
+            if (threadIdx.x < bcur) s_scale[threadIdx.x] = (float)dscal[1];
+            __syncthreads();
         } else {
-            float2* sm = reinterpret_cast<float2*>(smem_raw);
-            for (int e = threadIdx.x; e < nsm; e += blockDim.x) sm[e] = make_float2(0.f, 0.f);
+            subproblem_scales(g, sp, y, b0, bcur, s_bound, s_scale);
         }
-        __syncthreads();
 
-        for (int s = sp.y + team; s < sp.y + sp.z; s += nteam) {
-            int iz[JM], iy[JM];
-            float2 cz[JM], cy[JM];
-            load_axis<JM>(g, DI, s, iz, cz);
-            if constexpr (DIM > 1) load_axis<JM>(g, DY, s, iy, cy);
-            // local offsets of the footprint origin inside the tile
-            const int lz = __ldg(g.pos[DI] + s) - o[DI];
-            const int ly = (DIM > 1) ? __ldg(g.pos[DY] + s) - o[DY] : 0;
+        const int per_round = nwarps * NT;
+        for (int base_s = sp.y; base_s < sp.y + sp.z; base_s += per_round) {
+            const int s = base_s + warp * NT + team;
+            if (team >= NT || s >= sp.y + sp.z) continue;
+            const int lz = __ldg(g.pos[DI] + s) - o[DI] + k;
+            const float2 cz = __ldg(g.coef[DI] + (size_t)s * g.JP[DI] + k);
+            int ly = 0;
+            float2 cy[JM];
+            if constexpr (DIM > 1) {
+                ly = __ldg(g.pos[DY] + s) - o[DY];
+                const float2* src = g.coef[DY] + (size_t)s * g.JP[DY];
+#pragma unroll
+                for (int j = 0; j < JM; ++j)
+                    cy[j] = (j < g.J[DY]) ? __ldg(src + j) : make_float2(0.f, 0.f);
+            }
             const int lx = (DIM > 2) ? __ldg(g.pos[0] + s) - o[0] : 0;
             const float2* c0src = g.coef[0] + (size_t)s * g.JP[0];
             const int m = __ldg(g.perm + s);
-            for (int b = lane; b < bcur; b += G) {
-                const float2 yv = __ldg(y + (size_t)m * B + b0 + b);
+            for (int b = 0; b < bcur; ++b) {
+                const float sc = s_scale[b];
+                float2 v = cmulc(__ldg(y + (size_t)m * B + b0 + b), cz);
+                v.x *= sc;          // fixed-point scale applied once per point
+                v.y *= sc;
+                T* re = tile + b * ncell;
+                T* im = tile + nsm + b * ncell;
                 if constexpr (DIM == 1) {
-#pragma unroll
-                    for (int k = 0; k < JM; ++k)
-                        if (k < g.J[DI]) smem_add<DET>(smem_raw, (lz + k) * bcur + b, cmulc(yv, cz[k]), scale);
+                    atomicAdd(re + lz, Acc<DET>::fix(v.x, 1.f));
+                    atomicAdd(im + lz, Acc<DET>::fix(v.y, 1.f));
                 } else {
                     const int ni = (DIM > 2) ? J0 : 1;
 #pragma unroll 1
                     for (int i = 0; i < ni; ++i) {
-                        const float2 wi = (DIM > 2) ? cmulc(yv, __ldg(c0src + i)) : yv;
+                        const float2 wi = (DIM > 2) ? cmulc(v, __ldg(c0src + i)) : v;
                         const int ci = (DIM > 2) ? (lx + i) * Ty : 0;
 #pragma unroll
                         for (int j = 0; j < JM; ++j) {
                             if (j >= g.J[DY]) continue;
-                            const float2 wij = cmulc(wi, cy[j]);
-                            const int cj = (ci + ly + j) * Tz + lz;
-#pragma unroll
-                            for (int k = 0; k < JM; ++k) {
-                                if (k >= g.J[DI]) continue;
-                                smem_add<DET>(smem_raw, (cj + k) * bcur + b, cmulc(wij, cz[k]), scale);
-                            }
+                            const float2 w = cmulc(wi, cy[j]);
+                            const int cell = (ci + ly + j) * Tz + lz;
+                            atomicAdd(re + cell, Acc<DET>::fix(w.x, 1.f));
+                            atomicAdd(im + cell, Acc<DET>::fix(w.y, 1.f));
                         }
                     }
                 }
             }
         }
         __syncthreads();
+        flush_tile<DIM, DET, false>(g, o, inst, ncell, b0, bcur, tile, s_scale, grid, igrid);
+        __syncthreads();
+    }
+}
 
-        // flush the tile (with wrap-around) into the global grid
-        const size_t ibase = (size_t)inst * g.prodK;
-        for (int e = threadIdx.x; e < nsm; e += blockDim.x) {
-            const int b = e % bcur;
-            int cell = e / bcur;
-            int t[3] = {0, 0, 0};
+// ---------------------------------------------------------------------------
+// y2k, coil-teams (B >= 8): tile layout cell-major, coil fastest
+// ---------------------------------------------------------------------------
+template <int DIM, int JM, int G, bool DET>
+__global__ void __launch_bounds__(256) y2k_coil_kernel(Geom g, const float2* __restrict__ y,
+                                                       float2* __restrict__ grid,
+                                                       unsigned long long* __restrict__ igrid,
+                                                       int bc, const double* __restrict__ dscal) {
+    using T = typename Acc<DET>::T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float s_bound[64], s_scale[64];
+    const int4 sp = g.sub[blockIdx.x];
+    const int inst = sp.w;
+    int o[3];
+    tile_origin<DIM>(g, sp, o);
+    constexpr int DI = DIM - 1;
+    constexpr int DY = (DIM > 1) ? DIM - 2 : 0;
+    const int Tz = g.T[DI];
+    const int Ty = (DIM > 1) ? g.T[DY] : 1;
+    int ncell = 1;
 #pragma unroll
-            for (int d = DIM - 1; d >= 0; --d) {
-                t[d] = cell % g.T[d];
-                cell /= g.T[d];
-            }
-            size_t gc = 0;
+    for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
+    const int B = g.B;
+    const int team = threadIdx.x / G, lane = threadIdx.x % G, nteam = blockDim.x / G;
+    const int J0 = g.J[0];
+    T* tile = reinterpret_cast<T*>(smem_raw);
+
+    for (int b0 = 0; b0 < B; b0 += bc) {
+        const int bcur = min(bc, B - b0);
+        const int nsm = ncell * bcur;
+        for (int e = threadIdx.x; e < 2 * nsm; e += blockDim.x) tile[e] = 0;
+        if constexpr (DET) {
+            for (int b = threadIdx.x; b < bcur; b += blockDim.x) s_scale[b] = (float)dscal[1];
+            __syncthreads();
+        } else {
+            subproblem_scales(g, sp, y, b0, bcur, s_bound, s_scale);
+        }
+        T* re = tile;
+        T* im = tile + nsm;
+        for (int s = sp.y + team; s < sp.y + sp.z; s += nteam) {
+            int iz[JM], iy[JM];
+            float2 cz[JM], cy[JM];
+            load_axis<JM>(g, DI, s, iz, cz);
+            if constexpr (DIM > 1) load_axis<JM>(g, DY, s, iy, cy);
+            const int lz = __ldg(g.pos[DI] + s) - o[DI];
+            const int ly = (DIM > 1) ? __ldg(g.pos[DY] + s) - o[DY] : 0;
+            const int lx = (DIM > 2) ? __ldg(g.pos[0] + s) - o[0] : 0;
+            const float2* c0src = g.coef[0] + (size_t)s * g.JP[0];
+            const int m = __ldg(g.perm + s);
+            for (int b = lane; b < bcur; b += G) {
+                const float sc = s_scale[b];
+                float2 yv = __ldg(y + (size_t)m * B + b0 + b);
+                yv.x *= sc;         // fixed-point scale applied once per point
+                yv.y *= sc;
+                const int ni = (DIM > 2) ? J0 : 1;
+#pragma unroll 1
+                for (int i = 0; i < ni; ++i) {
+                    const float2 wi = (DIM > 2) ? cmulc(yv, __ldg(c0src + i)) : yv;
+                    const int ci = (DIM > 2) ? (lx + i) * Ty : 0;
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                int v = o[d] + t[d];
-                while (v >= g.K[d]) v -= g.K[d];
-                gc = gc * g.K[d] + v;
-            }
-            const size_t gi = (ibase + gc) * B + b0 + b;
-            if (DET) {
-                unsigned long long* sm = reinterpret_cast<unsigned long long*>(smem_raw);
-                const unsigned long long vx = sm[2 * e], vy = sm[2 * e + 1];
-                if (vx) atomicAdd(igrid + 2 * gi, vx);
-                if (vy) atomicAdd(igrid + 2 * gi + 1, vy);
-            } else {
-                const float2 v = reinterpret_cast<float2*>(smem_raw)[e];
-                if (v.x != 0.f || v.y != 0.f) atomicAdd(grid + gi, v);
+                    for (int j = 0; j < ((DIM > 1) ? JM : 1); ++j) {
+                        if (DIM > 1 && j >= g.J[DY]) continue;
+                        const float2 wij = (DIM > 1) ? cmulc(wi, cy[j]) : wi;
+                        const int cj = (DIM > 1) ? (ci + ly + j) * Tz + lz : lz;
+#pragma unroll
+                        for (int kk = 0; kk < JM; ++kk) {
+                            if (kk >= g.J[DI]) continue;
+                            const float2 w = cmulc(wij, cz[kk]);
+                            const int e = (cj + kk) * bcur + b;
+                            atomicAdd(re + e, Acc<DET>::fix(w.x, 1.f));
+                            atomicAdd(im + e, Acc<DET>::fix(w.y, 1.f));
+                        }
+                    }
+                }
             }
         }
+        __syncthreads();
+        flush_tile<DIM, DET, true>(g, o, inst, ncell, b0, bcur, tile, s_scale, grid, igrid);
         __syncthreads();
     }
 }

@@ -12,15 +12,41 @@ namespace nufft {
 inline int pick_team(int B) {
     if (B >= 32) return 32;
     if (B >= 8) return 8;
-    return 1;
+    return 1;   // z-teams
 }
 
+// ---------------------------------------------------------------------------
+// k2y
+// ---------------------------------------------------------------------------
 template <int DIM, int JM, int G>
 static void k2y_launch(const Geom& g, const float2* grid, float2* y, cudaStream_t s) {
     const int threads = 256;
-    const int64_t nthr = g.M * G;
-    const int64_t blocks = (nthr + threads - 1) / threads;
-    k2y_kernel<DIM, JM, G><<<(unsigned)blocks, threads, 0, s>>>(g, grid, y);
+    if constexpr (G == 1) {
+        if (g.kmethod == NUFFT_K2Y_TILE) {
+            int ncell = 1;
+            for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
+            const size_t smem = sizeof(float2) * ncell;
+            if (smem > 48 * 1024)
+                cudaFuncSetAttribute(k2y_tile_kernel<DIM, JM>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (g.nsub > 0)
+                k2y_tile_kernel<DIM, JM><<<(unsigned)g.nsub, threads, smem, s>>>(g, grid, y);
+        } else if (g.kmethod == NUFFT_K2Y_POINT) {
+            const int64_t blocks = (g.M + threads - 1) / threads;
+            if (g.B == 1)
+                k2y_point_kernel<DIM, JM><<<(unsigned)blocks, threads, 0, s>>>(g, grid, y);
+            else
+                k2y_coil_kernel<DIM, JM, 1><<<(unsigned)blocks, threads, 0, s>>>(g, grid, y);
+        } else {
+            const int TS = g.J[DIM - 1];
+            const int64_t nwarps = (g.M + (32 / TS) - 1) / (32 / TS);
+            const int64_t blocks = (nwarps * 32 + threads - 1) / threads;
+            k2y_zteam_kernel<DIM, JM><<<(unsigned)blocks, threads, 0, s>>>(g, grid, y);
+        }
+    } else {
+        const int64_t blocks = (g.M * G + threads - 1) / threads;
+        k2y_coil_kernel<DIM, JM, G><<<(unsigned)blocks, threads, 0, s>>>(g, grid, y);
+    }
 }
 
 template <int DIM, int JM>
@@ -42,22 +68,49 @@ static void k2y_jm(int jm, const Geom& g, const float2* grid, float2* y, cudaStr
     }
 }
 
+// ---------------------------------------------------------------------------
+// y2k
+// ---------------------------------------------------------------------------
+// Coils per shared-memory chunk: as many as fit in ~100 KB (two blocks per
+// SM), split into equal chunks, at most 64; one coil may use up to 200 KB.
+inline int coil_chunk(size_t cellbytes, int B, size_t* smem) {
+    const size_t target = 100 * 1024, big = 200 * 1024;
+    if (cellbytes > big) return 0;
+    int bmax = (int)std::min<size_t>(64, std::max<size_t>(1, target / cellbytes));
+    const int n = (B + bmax - 1) / bmax;
+    const int bc = (B + n - 1) / n;
+    *smem = cellbytes * bc;
+    return bc;
+}
+
 template <int DIM, int JM, int G, bool DET>
 static int y2k_launch(const Geom& g, const float2* y, float2* grid, unsigned long long* igrid,
                       const double* dscal, cudaStream_t s) {
+    if constexpr (G == 1 && !DET) {
+        if (g.ymethod == NUFFT_Y2K_GLOBAL) {
+            const int TS = g.J[DIM - 1];
+            const int64_t nwarps = (g.M + (32 / TS) - 1) / (32 / TS);
+            const int64_t blocks = (nwarps * 32 + 255) / 256;
+            y2k_global_kernel<DIM, JM><<<(unsigned)blocks, 256, 0, s>>>(g, y, grid);
+            return check_launch("y2k_global_kernel");
+        }
+    }
     int ncell = 1;
     for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
-    const size_t per = DET ? 16 : 8;
-    const size_t budget_small = 48 * 1024, budget_max = 200 * 1024;
-    size_t cellbytes = (size_t)ncell * per;
-    if (cellbytes > budget_max) {
+    const size_t per = DET ? 16 : 8;   // re + im accumulators per cell and coil
+    size_t smem = 0;
+    int bc = coil_chunk((size_t)ncell * per, (G == 1) ? std::min(g.B, 7) : g.B, &smem);
+    if (bc == 0) {
         set_error("y2k: gridding tile does not fit in shared memory; use a smaller bin shape");
         return NUFFT_EUNSUPPORTED;
     }
-    int bc = (int)std::max<size_t>(1, budget_small / cellbytes);
-    bc = std::min(bc, g.B);
-    size_t smem = cellbytes * bc;
-    auto kern = y2k_kernel<DIM, JM, G, DET>;
+    void (*kern)(Geom, const float2*, float2*, unsigned long long*, int, const double*);
+    if constexpr (G == 1) {
+        kern = (g.ymethod == NUFFT_Y2K_POINT) ? y2k_coil_kernel<DIM, JM, 1, DET>
+                                              : y2k_zteam_kernel<DIM, JM, DET>;
+    } else {
+        kern = y2k_coil_kernel<DIM, JM, G, DET>;
+    }
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);

@@ -54,8 +54,11 @@ struct Geom {
     const int* perm;             // sorted -> original point index
     const int* pos[3];           // first footprint index per axis, sorted order
     const float2* coef[3];       // conj(u) coefficients, sorted order, stride JP
+    const float* wpt;            // per point prod_d max_j |coef|, sorted order
     const int4* sub;             // gridding sub-problems: (bin, start, count, inst)
     int64_t nsub;
+    int kmethod;                 // k2y lane mapping (NUFFT_K2Y_*), resolved
+    int ymethod;                 // y2k lane mapping (NUFFT_Y2K_*), resolved
 };
 
 }  // namespace nufft
@@ -69,6 +72,7 @@ struct nufft_plan_s {
     int bs[3] = {0, 0, 0};
     int user_bs[3] = {0, 0, 0};
     int maxsub = 0, user_maxsub = 0;
+    int k2y_method = 0, y2k_method = 0;   // 0 = default for the geometry
     int device = 0;
     int num_sms = 0;
 
@@ -85,6 +89,7 @@ struct nufft_plan_s {
     int64_t* d_inst_start = nullptr;
     int* d_perm = nullptr;
     int* d_pos = nullptr;             // ndim * M
+    float* d_wpt = nullptr;           // M per-point weight bound prod_d max_j |coef|
     float2* d_coef = nullptr;         // sum_d M * JP[d]
     int4* d_sub = nullptr;
     int64_t nsub = 0;

@@ -165,7 +165,8 @@ __global__ void build_tables_kernel(const double* __restrict__ om, int64_t M, in
                                     const int* __restrict__ bin_start,
                                     int* __restrict__ perm, int* __restrict__ pos,
                                     float2* __restrict__ coef0, float2* __restrict__ coef1,
-                                    float2* __restrict__ coef2, unsigned int* __restrict__ wmax) {
+                                    float2* __restrict__ coef2, float* __restrict__ wpt,
+                                    unsigned int* __restrict__ wmax) {
     float2* coefs[3] = {coef0, coef1, coef2};
     for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
          m += (int64_t)gridDim.x * blockDim.x) {
@@ -191,6 +192,7 @@ __global__ void build_tables_kernel(const double* __restrict__ om, int64_t M, in
             for (int j = 0; j < g.JP[d]; ++j) dst[j] = (j < a.J) ? buf[j] : make_float2(0.f, 0.f);
             wprod *= amax;
         }
+        wpt[s] = wprod;
         atomicMax(wmax, __float_as_uint(wprod));
     }
 }
@@ -222,6 +224,7 @@ void free_points(nufft_plan_s* p) {
     cudaFree(p->d_inst_start); p->d_inst_start = nullptr;
     cudaFree(p->d_perm); p->d_perm = nullptr;
     cudaFree(p->d_pos); p->d_pos = nullptr;
+    cudaFree(p->d_wpt); p->d_wpt = nullptr;
     cudaFree(p->d_coef); p->d_coef = nullptr;
     cudaFree(p->d_sub); p->d_sub = nullptr;
     cudaFree(p->d_ybuf); p->d_ybuf = nullptr;
@@ -231,11 +234,14 @@ void free_points(nufft_plan_s* p) {
 }
 
 static void default_bins(const nufft_plan_s* p, int bs[3], int& maxsub) {
-    // cells per bin axis; the scatter tile is (bs + J - 1) per axis
+    // cells per bin axis; the gridding tile is (bs + J - 1) per axis.  Sub-
+    // problems hold at most 256 points, which keeps the 32-bit fixed-point
+    // rounding unit of the fast gridding mode below float32 resolution.
     for (int d = 0; d < 3; ++d) bs[d] = 1;
-    if (p->ndim == 1) { bs[0] = 1024; maxsub = 1024; }
-    else if (p->ndim == 2) { bs[0] = 32; bs[1] = 32; maxsub = 1024; }
-    else { bs[0] = 8; bs[1] = 8; bs[2] = 8; maxsub = 512; }
+    if (p->ndim == 1) { bs[0] = 1024; }
+    else if (p->ndim == 2) { bs[0] = bs[1] = (p->B >= 8) ? 16 : 32; }
+    else { bs[0] = bs[1] = 8; bs[2] = (p->B >= 8) ? 4 : 8; }
+    maxsub = 256;
     for (int d = 0; d < p->ndim; ++d) {
         if (p->user_bs[d] > 0) bs[d] = p->user_bs[d];
         bs[d] = std::min(bs[d], p->Kd[d]);
@@ -276,6 +282,7 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     int64_t Malloc = std::max<int64_t>(M, 1);
     NUFFT_CUDA_TRY(cudaMalloc(&p->d_perm, sizeof(int) * Malloc));
     NUFFT_CUDA_TRY(cudaMalloc(&p->d_pos, sizeof(int) * Malloc * nd));
+    NUFFT_CUDA_TRY(cudaMalloc(&p->d_wpt, sizeof(float) * Malloc));
     int64_t coef_elems = 0;
     int JP[3] = {0, 0, 0};
     for (int d = 0; d < nd; ++d) {
@@ -366,7 +373,7 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     if (M > 0) {
         build_tables_kernel<<<blocks, threads, 0, s>>>(d_om, M, nd, p->d_axc, d_tab, g, d_bin_of,
                                                        d_rank, d_start, p->d_perm, p->d_pos,
-                                                       c0, c1, c2, d_wmax);
+                                                       c0, c1, c2, p->d_wpt, d_wmax);
         TRY_TMP(cudaGetLastError());
     }
     const int bblocks = (int)std::min<int64_t>((nbins + threads - 1) / threads, 65535);

@@ -64,14 +64,16 @@ class NUFFT:
 
     # ------------------------------------------------------------------ plan
     def plan(self, om, Nd, Kd, Jd, ft_axes=None, batch=None, deterministic=False,
-             bins=None, max_sub_points=None):
+             bins=None, max_sub_points=None, autotune=False):
         """Plan for the points ``om`` (M x ndim radians).
 
         Argument checks follow helper.plan (src/_helper/helper.py:644-654):
         ``TypeError`` when Nd/Kd/Jd are not tuples, ``KeyError`` when their
         lengths differ.  ``deterministic=True`` selects the bitwise-reproducible
         gridding mode.  ``bins``/``max_sub_points`` override the gridding bin
-        shape (see ``pynufft_gb300.autotune``).  Returns 0.
+        shape; ``autotune=True`` applies the cached best setting for this
+        geometry and point density, or searches once (``pynufft_gb300.autotune``).
+        Returns 0.
         """
         self._check_shapes(Nd, Kd, Jd)
         ndim = len(Nd)
@@ -80,11 +82,14 @@ class NUFFT:
         B = 1 if batch is None else int(batch)
         if B < 1:
             raise ValueError('batch must be a positive integer')
-        return self._plan_common([om], Nd, Kd, Jd, batch, B, 1, deterministic, bins,
-                                 max_sub_points)
+        st = self._plan_common([om], Nd, Kd, Jd, batch, B, 1, deterministic, bins,
+                               max_sub_points)
+        if autotune:
+            self._autotune([om])
+        return st
 
     def plan_many(self, om_list, Nd, Kd, Jd, batch=None, deterministic=False, bins=None,
-                  max_sub_points=None):
+                  max_sub_points=None, autotune=False):
         """Plan ``len(om_list)`` independent instances that share Nd/Kd/Jd but
         have their own points (uneven M).  Every transform then runs all
         instances in the same kernel launches: x is (ninst,)+Nd[+(batch,)],
@@ -94,8 +99,19 @@ class NUFFT:
         if len(om_list) < 1:
             raise ValueError('om_list is empty')
         B = 1 if batch is None else int(batch)
-        return self._plan_common(list(om_list), Nd, Kd, Jd, batch, B, len(om_list),
-                                 deterministic, bins, max_sub_points)
+        st = self._plan_common(list(om_list), Nd, Kd, Jd, batch, B, len(om_list),
+                               deterministic, bins, max_sub_points)
+        if autotune:
+            self._autotune(list(om_list))
+        return st
+
+    def _autotune(self, oms):
+        from . import autotune as at
+        choice = at.cached(self)
+        if choice is not None:
+            at.apply(self, oms, choice)
+        else:
+            at.tune(self, oms if len(oms) > 1 else oms[0])
 
     @staticmethod
     def _check_shapes(Nd, Kd, Jd):
@@ -203,6 +219,18 @@ class NUFFT:
             self.release()
         except Exception:
             pass
+
+    K2Y_METHODS = {'zteam': 1, 'point': 2, 'tile': 3}
+    Y2K_METHODS = {'zteam': 1, 'point': 2, 'global': 3}
+
+    def set_methods(self, k2y=None, y2k=None):
+        """Choose the lane mapping of the interpolation/gridding kernels for
+        plans with fewer than 8 coils: k2y in {'tile', 'zteam', 'point'},
+        y2k in {'zteam', 'point', 'global'}; None keeps the default."""
+        km = 0 if k2y is None else self.K2Y_METHODS[k2y]
+        ym = 0 if y2k is None else self.Y2K_METHODS[y2k]
+        _lib.check(self._lib.nufft_plan_set_methods(self._plan, km, ym), 'set_methods')
+        self.methods = (k2y, y2k)
 
     def info(self):
         m, ns, by = c_int64(), c_int64(), c_int64()

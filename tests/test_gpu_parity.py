@@ -275,3 +275,41 @@ def test_full_size_3d_against_exact_nudft(NUFFT):
     lhs = np.vdot(y.astype(np.complex128), yr)
     rhs = np.prod(Kd) * np.vdot(x.astype(np.complex128), xa)
     assert abs(lhs - rhs) / abs(lhs) < 1e-5
+
+
+@pytest.mark.parametrize('case', ['plan_1d', 'plan_2d', 'plan_3d', 'plan_3d_aniso', 'plan_2d_J8'])
+@pytest.mark.parametrize('k2y,y2k', [('tile', 'zteam'), ('zteam', 'point'), ('point', 'global')])
+def test_every_lane_mapping_matches_reference(NUFFT, case, k2y, y2k):
+    g = load_golden(case)
+    A = NUFFT(0)
+    A.plan(g['om'], _tup(g['Nd']), _tup(g['Kd']), _tup(g['Jd']))
+    A.set_methods(k2y, y2k)
+    assert rel_l2(A.k2y(g['k']), g['k2y']) < TOL
+    assert rel_l2(A.y2k(g['y']), g['y2k']) < TOL
+    assert rel_l2(A.forward(g['x']), g['forward']) < TOL
+    assert rel_l2(A.adjoint(g['y']), g['adjoint']) < TOL
+
+
+@pytest.mark.parametrize('bins', [(4, 4), (16, 8), (64, 64)])
+def test_bin_shapes_do_not_change_results(NUFFT, bins):
+    g = load_golden('plan_2d')
+    A = NUFFT(0)
+    A.plan(g['om'], (32, 32), (64, 64), (6, 6), bins=bins, max_sub_points=64)
+    assert rel_l2(A.y2k(g['y']), g['y2k']) < TOL
+    assert rel_l2(A.k2y(g['k']), g['k2y']) < TOL
+
+
+def test_autotune_picks_a_setting_and_keeps_results(NUFFT, tmp_path, monkeypatch):
+    """The autotuner re-plans with the fastest candidate and caches it; the
+    transform is unchanged."""
+    from pynufft_gb300 import autotune
+    monkeypatch.setattr(autotune, 'CACHE', str(tmp_path / 'tune.json'))
+    g = load_golden('plan_3d')
+    A = NUFFT(0)
+    A.plan(g['om'], (12, 12, 12), (24, 24, 24), (6, 6, 6), autotune=True)
+    assert autotune.cached(A) is not None and A.tuned['ms'] > 0
+    assert rel_l2(A.forward(g['x']), g['forward']) < TOL
+    assert rel_l2(A.adjoint(g['y']), g['adjoint']) < TOL
+    B = NUFFT(0)
+    B.plan(g['om'], (12, 12, 12), (24, 24, 24), (6, 6, 6), autotune=True)   # from the cache
+    assert B.tuned == A.tuned
