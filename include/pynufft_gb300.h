@@ -98,7 +98,7 @@ int nufft_plan_set_bins(nufft_plan_t plan, const int* bin_shape, int max_sub_poi
 
 /* Lane mappings of the interpolation (k2y) and gridding (y2k) kernels for
  * plans with fewer than 8 coils (plans with 8 or more always split coils
- * across lanes).  0 keeps the default (tile / z-team).  Used by the
+ * across lanes).  0 keeps the default (one thread per point).  Used by the
  * autotuner; results are identical up to float32 rounding order. */
 #define NUFFT_K2Y_COIL  0   /* (internal) lanes over coils                    */
 #define NUFFT_K2Y_ZTEAM 1   /* J lanes per point along the innermost axis     */
@@ -152,6 +152,17 @@ int nufft_k2y2k(nufft_plan_t plan, const void* k, void* k_out, void* stream);
  * system ran; reading it synchronises `stream`. */
 int nufft_solve_cg(nufft_plan_t plan, const void* y, void* x, int maxiter,
                    double rtol, double atol, int* iters_out, void* stream);
+
+/* SENSE coil operators of the deprecated reference class
+ * (linalg/nufft_cpu.py:163-203).  nufft_set_sense copies coil maps of shape
+ * Nd + (batch,) (complex64, coil fastest; host or device pointer; NULL
+ * forgets them).  forward_one2many: single-coil image x (Nd) -> y (M, batch)
+ * = forward(x * maps), the map multiply fused into the sn/zero-pad pass.
+ * adjoint_many2one: y (M, batch) -> x (Nd) = mean over coils of
+ * conj(maps) * adjoint(y), fused into the crop pass.  Single-instance plans. */
+int nufft_set_sense(nufft_plan_t plan, const void* maps, int maps_on_device, void* stream);
+int nufft_forward_one2many(nufft_plan_t plan, const void* x, void* y, void* stream);
+int nufft_adjoint_many2one(nufft_plan_t plan, const void* y, void* x, void* stream);
 
 /* Trajectory gradient support: dy[m, d] = sum_n x_n (-i (n_d - N_d/2))
  * e^{-i om_m.(n - N/2)}, evaluated with the plan's interpolator as the

@@ -314,12 +314,46 @@ class OracleNUFFT:
     def selfadjoint(self, x):         # :201-214
         return self.xx2x(self.k2xx(self.k2y2k(self.xx2k(self.x2xx(x)))))
 
+    # ---- SENSE coil operators (linalg/nufft_cpu.py:177-203)
+    def forward_one2many(self, x, maps):
+        """forward(x[..., None] * maps): image Nd -> (M, B)."""
+        return np.stack([self._k2y1(self._xx2k1(self._x2xx1(x * maps[..., b])))
+                         for b in range(maps.shape[-1])], axis=-1)
+
+    def adjoint_many2one(self, y, maps):
+        """mean over coils of conj(maps) * adjoint(y)."""
+        xs = [self._x2xx1(self._k2xx1(self._y2k1(y[:, b]))) * np.conj(maps[..., b])
+              for b in range(maps.shape[-1])]
+        return np.mean(np.stack(xs, axis=-1), axis=-1)
+
+    def density_pipe(self, maxiter):
+        """Pipe's density compensation weights (linalg/solve_cpu.py:165-183):
+        W <- W / forward(adjoint(W)), W0 = 1, single coil."""
+        W = np.ones(self.M, dtype=np.complex64)
+        for _ in range(maxiter):
+            E = self._k2y1(self._xx2k1(self._x2xx1(self._x2xx1(self._k2xx1(self._y2k1(W))))))
+            W = W / E
+        return W
+
     def solve(self, y, solver='cg', maxiter=None, rtol=1e-5, atol=0.0,
               return_info=False):
         """solve(y, 'cg', maxiter): CG on the k-space normal operator spH.sp,
         x0 = 0, then k2xx(k) / sn (linalg/solve_cpu.py:256-288).  The CG
         recursion restates scipy.sparse.linalg.cg (scipy 1.18.1,
         sparse/linalg/_isolve/iterative.py) without a preconditioner."""
+        if solver == 'dc':
+            # linalg/solve_cpu.py:202-225: x = adjoint(W * y)
+            W = self.density_pipe(maxiter)
+            return self.adjoint(W * y if self.batch is None else W[:, None] * y)
+        if solver in ('lsqr', 'lsmr'):
+            # linalg/solve_cpu.py:226-251: scipy lsqr/lsmr on sp, then k2xx(k)/sn
+            import scipy.sparse.linalg as sla
+            fn = sla.lsqr if solver == 'lsqr' else sla.lsmr
+            kw = dict(atol=atol, btol=atol) if solver == 'lsqr' else dict(atol=atol, btol=atol)
+            k = fn(self.sp, np.asarray(y).ravel(), maxiter=maxiter, **kw)[0] \
+                if solver == 'lsmr' else fn(self.sp, np.asarray(y).ravel(), iter_lim=maxiter, **kw)[0]
+            xx = self._k2xx1(np.reshape(k, self.Kd))
+            return xx / self.sn
         if solver != 'cg':
             raise NotImplementedError(solver)
 

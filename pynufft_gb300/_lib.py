@@ -53,6 +53,9 @@ SIGNATURES = {
     'nufft_solve_cg': (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_double, c_double,
                                POINTER(c_int), c_void_p]),
     'nufft_forward_dom': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    'nufft_set_sense': (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
+    'nufft_forward_one2many': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    'nufft_adjoint_many2one': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 _lib = None

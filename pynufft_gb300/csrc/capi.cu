@@ -48,10 +48,15 @@ nufft::Geom nufft_plan_s::geom() const {
     g.sub = d_sub;
     g.nsub = nsub;
     // lane mappings: coil-teams for B >= 8; otherwise the plan's choice, with
-    // the shared-memory tile gather and z-team gridding as defaults
-    g.kmethod = (B >= 8) ? NUFFT_K2Y_COIL : (k2y_method ? k2y_method : NUFFT_K2Y_TILE);
-    g.ymethod = (B >= 8) ? NUFFT_Y2K_COIL : (y2k_method ? y2k_method : NUFFT_Y2K_ZTEAM);
-    if ((flags & NUFFT_FLAG_DETERMINISTIC) && g.ymethod == NUFFT_Y2K_GLOBAL) g.ymethod = NUFFT_Y2K_ZTEAM;
+    // one thread per point as the default for both (fastest in measurement
+    // on 2D radial and 3D uniform trajectories; the autotuner may pick others)
+    g.kmethod = (B >= 8) ? NUFFT_K2Y_COIL : (k2y_method ? k2y_method : NUFFT_K2Y_POINT);
+    g.ymethod = (B >= 8) ? NUFFT_Y2K_COIL : (y2k_method ? y2k_method : NUFFT_Y2K_POINT);
+    // the exact mode's 64-bit atomics favour the z-team mapping (fewer bank
+    // conflicts); it has no global-atomic variant
+    if ((flags & NUFFT_FLAG_DETERMINISTIC) && B < 8 &&
+        (y2k_method == 0 || g.ymethod == NUFFT_Y2K_GLOBAL))
+        g.ymethod = NUFFT_Y2K_ZTEAM;
     return g;
 }
 
@@ -171,12 +176,13 @@ int nufft_plan_destroy(nufft_plan_t p) {
     if (!p) return NUFFT_OK;
     free_points(p);
     free_cg(p);
-    if (p->fft_ok) cufftDestroy(p->fft);
+    fft_destroy(p);
     cudaFree(p->d_snd);
     cudaFree(p->d_axc);
     cudaFree(p->d_grid);
     cudaFree(p->d_igrid);
     cudaFree(p->d_dscal);
+    cudaFree(p->d_maps);
     delete p;
     return NUFFT_OK;
 }
@@ -343,6 +349,55 @@ int nufft_solve_cg(nufft_plan_t p, const void* y, void* x, int maxiter, double r
     }
     return solve_cg(p, (const float2*)y, (float2*)x, maxiter, rtol, atol, iters_out,
                     as_stream(stream));
+}
+
+int nufft_set_sense(nufft_plan_t p, const void* maps, int maps_on_device, void* stream) {
+    NUFFT_TRY(need_plan(p, "nufft_set_sense"));
+    if (p->ninst != 1) {
+        set_error("nufft_set_sense: coil maps need a single-instance plan");
+        return NUFFT_EUNSUPPORTED;
+    }
+    const size_t n = (size_t)p->prodN * p->B;
+    if (!maps) {   // reset_sense: forget the maps
+        cudaFree(p->d_maps);
+        p->d_maps = nullptr;
+        return NUFFT_OK;
+    }
+    if (!p->d_maps) {
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_maps, sizeof(float2) * n));
+        p->dev_bytes += sizeof(float2) * n;
+    }
+    NUFFT_CUDA_TRY(cudaMemcpyAsync(p->d_maps, maps, sizeof(float2) * n,
+                                   maps_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                   as_stream(stream)));
+    if (!maps_on_device) NUFFT_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+    return NUFFT_OK;
+}
+
+int nufft_forward_one2many(nufft_plan_t p, const void* x, void* y, void* stream) {
+    NUFFT_TRY(need_points(p, "nufft_forward_one2many"));
+    NUFFT_TRY(need_ptrs(x, y, "nufft_forward_one2many", p));
+    if (!p->d_maps) {
+        set_error("nufft_forward_one2many: nufft_set_sense has not been called");
+        return NUFFT_EINVAL;
+    }
+    cudaStream_t s = as_stream(stream);
+    NUFFT_TRY(launch_pad_sense(p, (const float2*)x, p->d_grid, s));
+    NUFFT_TRY(fft_exec(p, p->d_grid, -1, s));
+    return launch_k2y(p, p->d_grid, (float2*)y, s);
+}
+
+int nufft_adjoint_many2one(nufft_plan_t p, const void* y, void* x, void* stream) {
+    NUFFT_TRY(need_points(p, "nufft_adjoint_many2one"));
+    NUFFT_TRY(need_ptrs(x, y, "nufft_adjoint_many2one", p));
+    if (!p->d_maps) {
+        set_error("nufft_adjoint_many2one: nufft_set_sense has not been called");
+        return NUFFT_EINVAL;
+    }
+    cudaStream_t s = as_stream(stream);
+    NUFFT_TRY(launch_y2k(p, (const float2*)y, p->d_grid, s));
+    NUFFT_TRY(fft_exec(p, p->d_grid, +1, s));
+    return launch_crop_sense(p, p->d_grid, (float2*)x, s);
 }
 
 int nufft_forward_dom(nufft_plan_t p, const void* x, void* dy, void* stream) {

@@ -163,6 +163,79 @@ __global__ void crop_rows_kernel(ImgGeom g, const float2* __restrict__ grid, flo
   }
 }
 
+// SENSE coil expansion fused into x2xx + zero-pad (forward_one2many of the
+// deprecated reference class, linalg/nufft_cpu.py:177-189): the single-coil
+// image x (Nd) times each coil map (Nd, B) times sn, written into the
+// B-coil grid row.
+__global__ void pad_sense_rows_kernel(ImgGeom g, const float2* __restrict__ x,
+                                      const float2* __restrict__ maps, float2* __restrict__ grid,
+                                      int64_t rows) {
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    int64_t inst;
+    int n[3];
+    row_index(g, r, g.K, inst, n);
+    bool inside = true;
+    for (int d = 0; d < g.ndim - 1; ++d) inside = inside && (n[d] < g.N[d]);
+    const int last = g.ndim - 1;
+    const int KL = g.K[last], NL = g.N[last];
+    const int B = g.B;
+    float2* dst = grid + (size_t)r * KL * B;
+    if (!inside) {
+        for (int e = threadIdx.x; e < KL * B; e += blockDim.x) dst[e] = make_float2(0.f, 0.f);
+        continue;
+    }
+    float s_lead = 1.f;
+    for (int d = 0; d < last; ++d) s_lead *= __ldg(g.sn[d] + n[d]);
+    int64_t xrow = inst;
+    for (int d = 0; d < last; ++d) xrow = xrow * g.N[d] + n[d];
+    const float2* xs = x + (size_t)xrow * NL;
+    const float2* ms = maps + (size_t)(xrow - inst * (g.prodN / NL)) * NL * B;
+    for (int e = threadIdx.x; e < KL * B; e += blockDim.x) {
+        const int k = e / B;
+        float2 v = make_float2(0.f, 0.f);
+        if (k < NL) {
+            const float2 a = __ldg(xs + k), m = __ldg(ms + e);
+            const float sc = s_lead * __ldg(g.sn[last] + k);
+            v = make_float2(sc * (a.x * m.x - a.y * m.y), sc * (a.x * m.y + a.y * m.x));
+        }
+        dst[e] = v;
+    }
+  }
+}
+
+// Coil combination fused into crop + xx2x (adjoint_many2one of the
+// deprecated reference class, linalg/nufft_cpu.py:191-203):
+// x[n] = mean_b conj(map[n,b]) * grid[n,b] * sn[n] / prod(Kd).
+__global__ void crop_sense_rows_kernel(ImgGeom g, const float2* __restrict__ grid,
+                                       const float2* __restrict__ maps, float2* __restrict__ x,
+                                       float norm, int64_t rows) {
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    int64_t inst;
+    int n[3];
+    row_index(g, r, g.N, inst, n);
+    const int last = g.ndim - 1;
+    const int KL = g.K[last], NL = g.N[last];
+    const int B = g.B;
+    float s_lead = 1.f;
+    for (int d = 0; d < last; ++d) s_lead *= __ldg(g.sn[d] + n[d]);
+    int64_t krow = inst;
+    for (int d = 0; d < last; ++d) krow = krow * g.K[d] + n[d];
+    const float2* src = grid + (size_t)krow * KL * B;
+    const float2* ms = maps + (size_t)(r - inst * (g.prodN / NL)) * NL * B;
+    float2* dst = x + (size_t)r * NL;
+    for (int k = threadIdx.x; k < NL; k += blockDim.x) {
+        float ax = 0.f, ay = 0.f;
+        for (int b = 0; b < B; ++b) {
+            const float2 v = __ldg(src + (size_t)k * B + b), m = __ldg(ms + (size_t)k * B + b);
+            ax = fmaf(m.x, v.x, fmaf(m.y, v.y, ax));      // conj(m) * v
+            ay = fmaf(m.x, v.y, fmaf(-m.y, v.x, ay));
+        }
+        const float sc = norm * s_lead * __ldg(g.sn[last] + k) / (float)B;
+        dst[k] = make_float2(ax * sc, ay * sc);
+    }
+  }
+}
+
 static int64_t rows_of(const ImgGeom& g, const int* ext, int ninst) {
     int64_t r = ninst;
     for (int d = 0; d < g.ndim - 1; ++d) r *= ext[d];
@@ -206,31 +279,100 @@ int launch_crop(const nufft_plan_s* p, const float2* grid, float2* xx, bool appl
     return check_launch("crop_rows_kernel");
 }
 
-int fft_init(nufft_plan_s* p) {
-    int n[3] = {p->Kd[0], p->Kd[1], p->Kd[2]};
-    const int B = p->B;
-    int istride, idist, batch;
-    if (B == 1) {
-        istride = 1;
-        idist = (int)p->prodK;
-        batch = p->ninst;
-    } else {
-        istride = B;
-        idist = 1;
-        batch = B;  // executed once per instance
-    }
-    NUFFT_CUFFT_TRY(cufftPlanMany(&p->fft, p->ndim, n, n, istride, idist, n, istride, idist,
-                                  CUFFT_C2C, batch));
-    p->fft_ok = true;
+// cuFFT plans.  The general plan transforms all axes of every coil and
+// instance.  For one coil and one instance the zero padding is exploited:
+// the forward transform runs the (y[,z]) FFTs only on the first N0 slabs
+// (the others are zero) and then the x-axis FFTs; the inverse runs the x-axis
+// FFTs and then the (y[,z]) FFTs only on the N0 slabs the crop keeps.  All
+// plans share one work area.
+static int make_plan(cufftHandle* h, int rank, int* n, int stride, int dist, int batch,
+                     size_t* work) {
+    NUFFT_CUFFT_TRY(cufftCreate(h));
+    NUFFT_CUFFT_TRY(cufftSetAutoAllocation(*h, 0));
+    size_t ws = 0;
+    NUFFT_CUFFT_TRY(cufftMakePlanMany(*h, rank, n, n, stride, dist, n, stride, dist, CUFFT_C2C,
+                                      batch, &ws));
+    *work = std::max(*work, ws);
     return NUFFT_OK;
 }
 
+int launch_pad_sense(const nufft_plan_s* p, const float2* x, float2* grid, cudaStream_t s) {
+    ImgGeom g = img_geom(p);
+    const int64_t rows = rows_of(g, g.K, p->ninst);
+    pad_sense_rows_kernel<<<row_blocks(p, rows), row_threads(g.K[g.ndim - 1] * g.B), 0, s>>>(
+        g, x, p->d_maps, grid, rows);
+    return check_launch("pad_sense_rows_kernel");
+}
+
+int launch_crop_sense(const nufft_plan_s* p, const float2* grid, float2* x, cudaStream_t s) {
+    ImgGeom g = img_geom(p);
+    const float norm = (float)(1.0 / (double)p->prodK);
+    const int64_t rows = rows_of(g, g.N, p->ninst);
+    crop_sense_rows_kernel<<<row_blocks(p, rows), row_threads(g.N[g.ndim - 1]), 0, s>>>(
+        g, grid, p->d_maps, x, norm, rows);
+    return check_launch("crop_sense_rows_kernel");
+}
+
+int fft_init(nufft_plan_s* p) {
+    int n[3] = {p->Kd[0], p->Kd[1], p->Kd[2]};
+    const int B = p->B;
+    size_t work = 0;
+    if (B == 1) {
+        NUFFT_TRY(make_plan(&p->fft, p->ndim, n, 1, (int)p->prodK, p->ninst, &work));
+    } else {
+        NUFFT_TRY(make_plan(&p->fft, p->ndim, n, B, 1, B, &work));   // once per instance
+    }
+    p->fft_ok = true;
+    if (B == 1 && p->ninst == 1 && p->ndim >= 2 && p->Nd[0] < p->Kd[0]) {
+        const int slab = (int)(p->prodK / p->Kd[0]);
+        NUFFT_TRY(make_plan(&p->fft_slab, p->ndim - 1, n + 1, 1, slab, p->Nd[0], &work));
+        NUFFT_TRY(make_plan(&p->fft_x, 1, n, slab, 1, slab, &work));
+        p->fft_pruned = true;
+    }
+    if (work > 0) {
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_fftwork, work));
+        p->dev_bytes += work;
+    }
+    NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft, p->d_fftwork));
+    if (p->fft_pruned) {
+        NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_slab, p->d_fftwork));
+        NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_x, p->d_fftwork));
+    }
+    return NUFFT_OK;
+}
+
+void fft_destroy(nufft_plan_s* p) {
+    if (p->fft_ok) cufftDestroy(p->fft);
+    if (p->fft_pruned) {
+        cufftDestroy(p->fft_slab);
+        cufftDestroy(p->fft_x);
+    }
+    p->fft_ok = p->fft_pruned = false;
+    cudaFree(p->d_fftwork);
+    p->d_fftwork = nullptr;
+}
+
+// direction < 0: forward (numpy fftn sign); > 0: inverse, unnormalised.
+// After an inverse transform of a single-coil plan only the first Nd[0]
+// slabs hold the transform (the crop reads nothing else).
 int fft_exec(nufft_plan_s* p, float2* grid, int direction, cudaStream_t s) {
-    NUFFT_CUFFT_TRY(cufftSetStream(p->fft, s));
     const int dir = (direction < 0) ? CUFFT_FORWARD : CUFFT_INVERSE;
+    cufftComplex* gc = reinterpret_cast<cufftComplex*>(grid);
+    if (p->fft_pruned) {
+        NUFFT_CUFFT_TRY(cufftSetStream(p->fft_slab, s));
+        NUFFT_CUFFT_TRY(cufftSetStream(p->fft_x, s));
+        if (dir == CUFFT_FORWARD) {
+            NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_slab, gc, gc, dir));
+            NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_x, gc, gc, dir));
+        } else {
+            NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_x, gc, gc, dir));
+            NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_slab, gc, gc, dir));
+        }
+        return NUFFT_OK;
+    }
+    NUFFT_CUFFT_TRY(cufftSetStream(p->fft, s));
     if (p->B == 1 || p->ninst == 1) {
-        NUFFT_CUFFT_TRY(cufftExecC2C(p->fft, reinterpret_cast<cufftComplex*>(grid),
-                                     reinterpret_cast<cufftComplex*>(grid), dir));
+        NUFFT_CUFFT_TRY(cufftExecC2C(p->fft, gc, gc, dir));
     } else {
         for (int i = 0; i < p->ninst; ++i) {
             cufftComplex* g = reinterpret_cast<cufftComplex*>(grid + (size_t)i * p->prodK * p->B);

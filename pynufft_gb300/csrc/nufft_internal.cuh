@@ -81,6 +81,7 @@ struct nufft_plan_s {
     nufft::AxisConst* d_axc = nullptr;
     float2* d_grid = nullptr;         // ninst * prodK * B oversampled grid workspace
     float2* d_ybuf = nullptr;         // M * B sample workspace (selfadjoint, CG)
+    float2* d_maps = nullptr;         // coil sensitivities Nd x B (nufft_set_sense)
     size_t ybuf_elems = 0;
 
     // point data (valid after nufft_set_points)
@@ -111,8 +112,11 @@ struct nufft_plan_s {
     int cg_maxiter = -1, cg_chunk = 0;
     double cg_rtol = 0, cg_atol = 0;
 
-    cufftHandle fft = 0;
-    bool fft_ok = false;
+    cufftHandle fft = 0;              // all axes, every coil / instance
+    cufftHandle fft_slab = 0;         // (y[,z]) FFTs on the first Nd[0] slabs
+    cufftHandle fft_x = 0;            // x-axis FFTs over all slabs
+    bool fft_ok = false, fft_pruned = false;
+    void* d_fftwork = nullptr;        // shared cuFFT work area
     size_t dev_bytes = 0;
 
     nufft::Geom geom() const;
@@ -171,7 +175,10 @@ int launch_pad(const nufft_plan_s* p, const float2* xx, float2* grid, bool apply
 int launch_crop(const nufft_plan_s* p, const float2* grid, float2* xx, bool apply_sn,
                 bool divide_sn, cudaStream_t s);
 int fft_exec(nufft_plan_s* p, float2* grid, int direction, cudaStream_t s);
+int launch_pad_sense(const nufft_plan_s* p, const float2* x, float2* grid, cudaStream_t s);
+int launch_crop_sense(const nufft_plan_s* p, const float2* grid, float2* x, cudaStream_t s);
 int fft_init(nufft_plan_s* p);
+void fft_destroy(nufft_plan_s* p);
 
 // cg.cu
 int solve_cg(nufft_plan_s* p, const float2* y, float2* x, int maxiter, double rtol,

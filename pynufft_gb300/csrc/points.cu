@@ -240,7 +240,7 @@ static void default_bins(const nufft_plan_s* p, int bs[3], int& maxsub) {
     for (int d = 0; d < 3; ++d) bs[d] = 1;
     if (p->ndim == 1) { bs[0] = 1024; }
     else if (p->ndim == 2) { bs[0] = bs[1] = (p->B >= 8) ? 16 : 32; }
-    else { bs[0] = bs[1] = 8; bs[2] = (p->B >= 8) ? 4 : 8; }
+    else { bs[0] = bs[1] = 8; bs[2] = (p->B >= 8) ? 4 : 16; }
     maxsub = 256;
     for (int d = 0; d < p->ndim; ++d) {
         if (p->user_bs[d] > 0) bs[d] = p->user_bs[d];

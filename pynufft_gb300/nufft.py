@@ -338,6 +338,71 @@ class NUFFT:
     xx2k_one2one = xx2k
     k2xx_one2one = k2xx
 
+    # ---- SENSE coil operators (deprecated reference class, linalg/nufft_cpu.py:163-203)
+    def set_sense(self, coil_profile):
+        """Coil sensitivities of shape Nd + (batch,) for forward_one2many /
+        adjoint_many2one."""
+        torch = _torch()
+        if self.batch is None:
+            raise ValueError('set_sense needs a plan with batch = number of coils')
+        shape = self.Nd + (self.batch,)
+        if tuple(coil_profile.shape) != shape:
+            raise ValueError(f'coil_profile must have shape {shape}')
+        if isinstance(coil_profile, torch.Tensor) and coil_profile.is_cuda:
+            m = coil_profile.to(self.device, torch.complex64).contiguous()
+            self._maps = m
+            ptr, on_dev = m.data_ptr(), 1
+        else:
+            m = numpy.ascontiguousarray(numpy.asarray(coil_profile), dtype=numpy.complex64)
+            self._maps = m
+            ptr, on_dev = m.ctypes.data, 0
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.nufft_set_sense(self._plan, c_void_p(ptr), on_dev, self._stream()),
+                       'set_sense')
+
+    def reset_sense(self):
+        """All-ones coil maps (the reference's reset_sense)."""
+        self.set_sense(numpy.ones(self.Nd + (self.batch,), dtype=numpy.complex64))
+
+    def forward_one2many(self, x):
+        """y = forward(x * coil maps): image Nd -> samples (M, batch)."""
+        torch = _torch()
+        lead = (self.ninst,) if self.ninst > 1 else ()
+        if self.batch is None or self.ninst > 1:
+            raise ValueError('forward_one2many needs a single-instance batch plan')
+        if isinstance(x, torch.Tensor):
+            if tuple(x.shape) != self.Nd:
+                raise ValueError(f'expected shape {self.Nd}')
+            d = x.to(self.device, torch.complex64).contiguous()
+            how = ('cuda', None) if x.is_cuda else ('cpu', x.is_pinned())
+        else:
+            a = numpy.ascontiguousarray(numpy.asarray(x), dtype=numpy.complex64)
+            if a.shape != self.Nd:
+                raise ValueError(f'expected shape {self.Nd}')
+            d, how = torch.from_numpy(a).to(self.device), ('numpy', None)
+        out = self._empty('y')
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.nufft_forward_one2many(self._plan, c_void_p(d.data_ptr()),
+                                                        c_void_p(out.data_ptr()), self._stream()),
+                       'forward_one2many')
+        return self._out(out, how)
+
+    def adjoint_many2one(self, y):
+        """x = mean over coils of conj(maps) * adjoint(y): (M, batch) -> Nd."""
+        torch = _torch()
+        if self.batch is None or self.ninst > 1:
+            raise ValueError('adjoint_many2one needs a single-instance batch plan')
+        d, how = self._in(y, 'y')
+        out = torch.empty(self.Nd, dtype=torch.complex64, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.nufft_adjoint_many2one(self._plan, c_void_p(d.data_ptr()),
+                                                        c_void_p(out.data_ptr()), self._stream()),
+                       'adjoint_many2one')
+        return self._out(out, how)
+
+    def selfadjoint_one2many2one(self, x):
+        return self.adjoint_many2one(self.forward_one2many(x))
+
     def forward_dom(self, x):
         """d y / d om: an (ndim, M[, batch]) array with
         dy[d, m] = sum_n x_n (-i (n_d - N_d/2)) exp(-i om_m . (n - N/2)),
@@ -352,19 +417,20 @@ class NUFFT:
                        'forward_dom')
         return self._out(out, how)
 
-    def solve(self, y, solver=None, *args, maxiter=None, rtol=1e-5, atol=0.0,
-              return_info=False, **kwargs):
+    def solve(self, y, solver=None, *args, **kwargs):
         """solve(y, 'cg', maxiter=...) (linalg/solve_cpu.py:256-288 via
         nufft/_nufft_class_methods_cpu.py:150-166): CG on the k-space normal
         operator, x0 = 0, scipy's rtol/atol stopping rule, then k2xx(k)/sn.
-        Other reference solvers are listed in ``pynufft_gb300.solvers``."""
+        'dc', 'lsqr' and 'lsmr' are in ``pynufft_gb300.solvers``."""
         if solver is None:
             raise ValueError('solver must be given, e.g. solve(y, "cg", maxiter=20)')
         if solver != 'cg':
             from . import solvers
-            return solvers.solve(self, y, solver, *args, maxiter=maxiter, **kwargs)
-        if kwargs.get('tol') is not None:
-            rtol = kwargs.pop('tol')
+            return solvers.solve(self, y, solver, *args, **kwargs)
+        maxiter = kwargs.pop('maxiter', args[0] if args else None)
+        rtol = kwargs.pop('rtol', kwargs.pop('tol', 1e-5))
+        atol = kwargs.pop('atol', 0.0)
+        return_info = kwargs.pop('return_info', False)
         torch = _torch()
         d, how = self._in(y, 'y')
         out = self._empty('x')

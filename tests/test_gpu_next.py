@@ -1,0 +1,73 @@
+"""The callers either side of the hot path: SENSE coil operators
+(forward_one2many / adjoint_many2one), density compensation ('dc') and the
+least-squares solvers ('lsqr', 'lsmr'), against the oracle."""
+import numpy as np
+import pytest
+
+from oracle.nufft_oracle import OracleNUFFT, rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def cplx(rng, shape):
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+
+
+@pytest.mark.parametrize('Nd,Kd,Jd,B', [((32, 32), (64, 64), (6, 6), 4),
+                                        ((12, 14, 10), (24, 28, 20), (6, 6, 6), 8)])
+def test_sense_operators_match_oracle(Nd, Kd, Jd, B):
+    from pynufft_gb300 import NUFFT
+    rng = np.random.default_rng(0)
+    M = 900
+    om = rng.uniform(-np.pi, np.pi, (M, len(Nd)))
+    maps = cplx(rng, Nd + (B,))
+    A = NUFFT(0)
+    A.plan(om, Nd, Kd, Jd, batch=B)
+    A.set_sense(maps)
+    O = OracleNUFFT()
+    O.plan(om, Nd, Kd, Jd)
+    x = cplx(rng, Nd)
+    y = cplx(rng, (M, B))
+    assert rel_l2(A.forward_one2many(x), O.forward_one2many(x, maps)) < TOL
+    assert rel_l2(A.adjoint_many2one(y), O.adjoint_many2one(y, maps)) < TOL
+    # the fused operators equal the plain batch path with the maps applied outside
+    yb = A.forward(x[..., None] * maps)
+    assert rel_l2(A.forward_one2many(x), yb) < 1e-6
+    A.reset_sense()
+    assert rel_l2(A.forward_one2many(x), A.forward(np.repeat(x[..., None], B, -1))) < 1e-6
+
+
+def test_density_compensation_matches_oracle():
+    from pynufft_gb300 import NUFFT
+    from pynufft_gb300.trajectories import radial_2d
+    rng = np.random.default_rng(1)
+    om = radial_2d(64, 128)
+    y = cplx(rng, (om.shape[0],))
+    A = NUFFT(0)
+    A.plan(om, (64, 64), (128, 128), (6, 6))
+    O = OracleNUFFT()
+    O.plan(om, (64, 64), (128, 128), (6, 6))
+    x = A.solve(y, 'dc', maxiter=5)
+    assert rel_l2(x, O.solve(y, 'dc', maxiter=5)) < 1e-4
+
+
+@pytest.mark.parametrize('solver', ['lsqr', 'lsmr'])
+def test_least_squares_solvers_match_scipy_on_the_oracle(solver):
+    """Fixed iteration count (atol = btol = 0): float32 vectors on the GPU vs
+    scipy's float64 recursion on the reference CSR."""
+    from pynufft_gb300 import NUFFT
+    rng = np.random.default_rng(2)
+    om = rng.uniform(-np.pi, np.pi, (1500, 2))
+    y = cplx(rng, (1500,))
+    A = NUFFT(0)
+    A.plan(om, (24, 24), (48, 48), (6, 6))
+    O = OracleNUFFT()
+    O.plan(om, (24, 24), (48, 48), (6, 6))
+    x, itn, _ = getattr(__import__('pynufft_gb300.solvers', fromlist=['x']), solver)(
+        A, y, iter_lim=8, atol=0.0, btol=0.0, return_info=True)
+    assert itn == 8
+    ref = O.solve(y, solver, maxiter=8, atol=0.0)
+    assert rel_l2(x, ref) < 1e-3, rel_l2(x, ref)
+    x2 = A.solve(y, solver, iter_lim=8, atol=0.0, btol=0.0)
+    assert rel_l2(x2, x) < 1e-6
