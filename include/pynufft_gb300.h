@@ -164,6 +164,25 @@ int nufft_set_sense(nufft_plan_t plan, const void* maps, int maps_on_device, voi
 int nufft_forward_one2many(nufft_plan_t plan, const void* x, void* y, void* stream);
 int nufft_adjoint_many2one(nufft_plan_t plan, const void* y, void* x, void* stream);
 
+/* Gridding (y2k) with the exact 64-bit fixed-point accumulation of the
+ * deterministic mode, for callers that cannot allocate device memory while
+ * they run: applications that hand all GPU memory to their own pool up front
+ * (where a stray cudaMalloc can fail or fragment the pool) and
+ * latency-critical code that cannot afford cudaMalloc/cudaFree (cudaFree
+ * synchronises the whole device).  No counterpart in the reference.
+ * It allocates nothing: its accumulators live in a scratch array compiled
+ * into the library (NUFFT_STATIC_SCRATCH_CELLS grid cells, 16 MiB, held on
+ * every GPU that loads the library until the process exits), and plans whose
+ * ninst * prod(Kd) * batch exceeds that size are rejected with NUFFT_EINVAL.
+ * The first call on a device looks the scratch address up for that device
+ * (the device must be current); make that first call before any stream
+ * capture.  All calls share the scratch, which keeps the last call's
+ * contents (each call clears it first): calls that overlap on the GPU, on
+ * different streams or threads, race.  Works on any plan; the result equals
+ * nufft_y2k on a plan created with NUFFT_FLAG_DETERMINISTIC. */
+#define NUFFT_STATIC_SCRATCH_CELLS (1u << 20)
+int nufft_y2k_exact_static(nufft_plan_t plan, const void* y, void* k, void* stream);
+
 /* Trajectory gradient support: dy[m, d] = sum_n x_n (-i (n_d - N_d/2))
  * e^{-i om_m.(n - N/2)}, evaluated with the plan's interpolator as the
  * forward transform of (-i (n_d - N_d/2)) x.  dy is ndim consecutive (M,batch)

@@ -54,6 +54,7 @@ SIGNATURES = {
                                POINTER(c_int), c_void_p]),
     'nufft_forward_dom': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     'nufft_set_sense': (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
+    'nufft_y2k_exact_static': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     'nufft_forward_one2many': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     'nufft_adjoint_many2one': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
 }

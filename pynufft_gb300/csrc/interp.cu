@@ -138,4 +138,25 @@ int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s) {
     return check_launch("fixed_to_float_kernel");
 }
 
+// Exact (fixed-point) gridding into `grid` using caller-provided scratch:
+// acc holds 2 * ninst * prodK * B accumulators, scal 2 + 1024 doubles.
+// Allocates nothing.
+int launch_y2k_exact_into(const nufft_plan_s* p, const float2* y, float2* grid,
+                          unsigned long long* acc, double* scal, cudaStream_t s) {
+    const size_t ncells = (size_t)p->ninst * p->prodK * p->B;
+    Geom g = p->geom();
+    g.ymethod = (p->B >= 8) ? NUFFT_Y2K_COIL : NUFFT_Y2K_ZTEAM;
+    NUFFT_CUDA_TRY(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * 2 * ncells, s));
+    const int64_t ny = p->M * (int64_t)p->B;
+    const int nparts = 1024;
+    abs_sum_partial_kernel<<<nparts, 256, 0, s>>>(y, ny, scal + 2);
+    NUFFT_TRY(check_launch("abs_sum_partial_kernel"));
+    fixed_scale_kernel<<<1, 256, 0, s>>>(scal + 2, nparts, p->wmax, scal);
+    NUFFT_TRY(check_launch("fixed_scale_kernel"));
+    if (p->M > 0) NUFFT_TRY(y2k_dim<true>(p, g, y, nullptr, acc, scal, s));
+    const int blocks = (int)std::min<size_t>((ncells + 255) / 256, (size_t)p->num_sms * 16);
+    fixed_to_float_kernel<<<std::max(blocks, 1), 256, 0, s>>>(acc, (int64_t)ncells, scal, grid);
+    return check_launch("fixed_to_float_kernel");
+}
+
 }  // namespace nufft
