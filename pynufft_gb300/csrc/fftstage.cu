@@ -52,28 +52,46 @@ __device__ __forceinline__ float sn_of(const ImgGeom& g, const int (&n)[3]) {
 // Row-wise kernels: one block per row of the last axis (all other indices
 // fixed per block), threads along the row, so index arithmetic is one
 // division chain per block and the row's accesses are contiguous.
-__device__ __forceinline__ void row_index(const ImgGeom& g, int64_t r, const int* ext,
-                                          int64_t& inst, int (&n)[3]) {
-    // r enumerates (inst, i0[, i1]) over the extents ext of the leading axes
-    n[0] = n[1] = n[2] = 0;
-    for (int d = g.ndim - 2; d >= 0; --d) {
-        n[d] = (int)(r % ext[d]);
-        r /= ext[d];
+template <int DIM>
+__device__ __forceinline__ void row_index(int64_t r64, int e0, int e1, int64_t& inst, int& n0,
+                                          int& n1) {
+    // r enumerates (inst, i0[, i1]) over the extents (e0[, e1]) of the
+    // leading axes; rows number fewer than 2^31, so 32-bit unsigned division
+    // suffices.  Scalars only: no local-memory copies of parameter arrays.
+    unsigned r = (unsigned)r64;
+    n0 = n1 = 0;
+    if (DIM == 3) {
+        const unsigned q = r / (unsigned)e1;
+        n1 = (int)(r - q * (unsigned)e1);
+        r = q;
+    }
+    if (DIM >= 2) {
+        const unsigned q = r / (unsigned)e0;
+        n0 = (int)(r - q * (unsigned)e0);
+        r = q;
     }
     inst = r;
 }
 
+template <int DIM>
+__device__ __forceinline__ float lead_sn(const float* sn0, const float* sn1, int n0, int n1) {
+    float s = 1.f;
+    if (DIM >= 2) s *= __ldg(sn0 + n0);
+    if (DIM == 3) s *= __ldg(sn1 + n1);
+    return s;
+}
+
+template <int DIM>
 __global__ void scale_rows_kernel(ImgGeom g, const float2* __restrict__ in, float2* __restrict__ out,
                                   int64_t rows) {
   for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
     int64_t inst;
-    int n[3];
-    row_index(g, r, g.N, inst, n);
-    const int L = g.N[g.ndim - 1];
+    int n[3] = {0, 0, 0};
+    row_index<DIM>(r, g.N[0], g.N[1], inst, n[0], n[1]);
+    const int L = g.N[DIM - 1];
     const int B = g.B;
-    float s_lead = 1.f;
-    for (int d = 0; d < g.ndim - 1; ++d) s_lead *= __ldg(g.sn[d] + n[d]);
-    const float* snl = g.sn[g.ndim - 1];
+    const float s_lead = lead_sn<DIM>(g.sn[0], g.sn[1], n[0], n[1]);
+    const float* snl = g.sn[DIM - 1];
     const size_t base = (size_t)r * L * B;
     for (int e = threadIdx.x; e < L * B; e += blockDim.x) {
         const int k = (B == 1) ? e : e / B;
@@ -86,15 +104,17 @@ __global__ void scale_rows_kernel(ImgGeom g, const float2* __restrict__ in, floa
 
 // grid row = x row * (sn if apply_sn) * (-i (n_a - N_a/2) if dom_axis == a),
 // zero outside the Nd corner
+template <int DIM>
 __global__ void pad_rows_kernel(ImgGeom g, const float2* __restrict__ xx, float2* __restrict__ grid,
                                 int apply_sn, int dom_axis, int64_t rows) {
   for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
     int64_t inst;
-    int n[3];
-    row_index(g, r, g.K, inst, n);
+    int n[3] = {0, 0, 0};
+    row_index<DIM>(r, g.K[0], g.K[1], inst, n[0], n[1]);
     bool inside = true;
-    for (int d = 0; d < g.ndim - 1; ++d) inside = inside && (n[d] < g.N[d]);
-    const int last = g.ndim - 1;
+#pragma unroll
+    for (int d = 0; d < DIM - 1; ++d) inside = inside && (n[d] < g.N[d]);
+    constexpr int last = DIM - 1;
     const int KL = g.K[last], NL = g.N[last];
     const int B = g.B;
     float2* dst = grid + (size_t)r * KL * B;
@@ -102,13 +122,13 @@ __global__ void pad_rows_kernel(ImgGeom g, const float2* __restrict__ xx, float2
         for (int e = threadIdx.x; e < KL * B; e += blockDim.x) dst[e] = make_float2(0.f, 0.f);
         continue;
     }
-    float s_lead = 1.f;
-    if (apply_sn)
-        for (int d = 0; d < last; ++d) s_lead *= __ldg(g.sn[d] + n[d]);
+    const float s_lead = apply_sn ? lead_sn<DIM>(g.sn[0], g.sn[1], n[0], n[1]) : 1.f;
     float a_lead = 0.f;
-    if (dom_axis >= 0 && dom_axis < last) a_lead = (float)n[dom_axis] - 0.5f * (float)g.N[dom_axis];
+    if (DIM >= 2 && dom_axis == 0) a_lead = (float)n[0] - 0.5f * (float)g.N[0];
+    if (DIM == 3 && dom_axis == 1) a_lead = (float)n[1] - 0.5f * (float)g.N[1];
     int64_t xrow = inst;
-    for (int d = 0; d < last; ++d) xrow = xrow * g.N[d] + n[d];
+    if (DIM >= 2) xrow = xrow * g.N[0] + n[0];
+    if (DIM == 3) xrow = xrow * g.N[1] + n[1];
     const float2* src = xx + (size_t)xrow * NL * B;
     for (int e = threadIdx.x; e < KL * B; e += blockDim.x) {
         const int k = (B == 1) ? e : e / B;
@@ -131,18 +151,19 @@ __global__ void pad_rows_kernel(ImgGeom g, const float2* __restrict__ xx, float2
 }
 
 // x row = grid row (first N of the last axis) / prod(Kd) * (sn if apply_sn) / (sn if divide_sn)
+template <int DIM>
 __global__ void crop_rows_kernel(ImgGeom g, const float2* __restrict__ grid, float2* __restrict__ xx,
                                  int apply_sn, int divide_sn, float norm, int64_t rows) {
   for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
     int64_t inst;
-    int n[3];
-    row_index(g, r, g.N, inst, n);
-    const int last = g.ndim - 1;
+    int n[3] = {0, 0, 0};
+    row_index<DIM>(r, g.N[0], g.N[1], inst, n[0], n[1]);
+    constexpr int last = DIM - 1;
     const int KL = g.K[last], NL = g.N[last];
     const int B = g.B;
-    float s_lead = 1.f;
-    for (int d = 0; d < last; ++d) s_lead *= __ldg(g.sn[d] + n[d]);
+    const float s_lead = lead_sn<DIM>(g.sn[0], g.sn[1], n[0], n[1]);
     int64_t krow = inst;
+#pragma unroll
     for (int d = 0; d < last; ++d) krow = krow * g.K[d] + n[d];
     const float2* src = grid + (size_t)krow * KL * B;
     float2* dst = xx + (size_t)r * NL * B;
@@ -167,16 +188,18 @@ __global__ void crop_rows_kernel(ImgGeom g, const float2* __restrict__ grid, flo
 // deprecated reference class, linalg/nufft_cpu.py:177-189): the single-coil
 // image x (Nd) times each coil map (Nd, B) times sn, written into the
 // B-coil grid row.
+template <int DIM>
 __global__ void pad_sense_rows_kernel(ImgGeom g, const float2* __restrict__ x,
                                       const float2* __restrict__ maps, float2* __restrict__ grid,
                                       int64_t rows) {
   for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
     int64_t inst;
-    int n[3];
-    row_index(g, r, g.K, inst, n);
+    int n[3] = {0, 0, 0};
+    row_index<DIM>(r, g.K[0], g.K[1], inst, n[0], n[1]);
     bool inside = true;
-    for (int d = 0; d < g.ndim - 1; ++d) inside = inside && (n[d] < g.N[d]);
-    const int last = g.ndim - 1;
+#pragma unroll
+    for (int d = 0; d < DIM - 1; ++d) inside = inside && (n[d] < g.N[d]);
+    constexpr int last = DIM - 1;
     const int KL = g.K[last], NL = g.N[last];
     const int B = g.B;
     float2* dst = grid + (size_t)r * KL * B;
@@ -189,7 +212,7 @@ __global__ void pad_sense_rows_kernel(ImgGeom g, const float2* __restrict__ x,
     int64_t xrow = inst;
     for (int d = 0; d < last; ++d) xrow = xrow * g.N[d] + n[d];
     const float2* xs = x + (size_t)xrow * NL;
-    const float2* ms = maps + (size_t)(xrow - inst * (g.prodN / NL)) * NL * B;
+    const float2* ms = maps + (size_t)xrow * NL * B;      // single-instance plans only
     for (int e = threadIdx.x; e < KL * B; e += blockDim.x) {
         const int k = e / B;
         float2 v = make_float2(0.f, 0.f);
@@ -206,22 +229,23 @@ __global__ void pad_sense_rows_kernel(ImgGeom g, const float2* __restrict__ x,
 // Coil combination fused into crop + xx2x (adjoint_many2one of the
 // deprecated reference class, linalg/nufft_cpu.py:191-203):
 // x[n] = mean_b conj(map[n,b]) * grid[n,b] * sn[n] / prod(Kd).
+template <int DIM>
 __global__ void crop_sense_rows_kernel(ImgGeom g, const float2* __restrict__ grid,
                                        const float2* __restrict__ maps, float2* __restrict__ x,
                                        float norm, int64_t rows) {
   for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
     int64_t inst;
-    int n[3];
-    row_index(g, r, g.N, inst, n);
-    const int last = g.ndim - 1;
+    int n[3] = {0, 0, 0};
+    row_index<DIM>(r, g.N[0], g.N[1], inst, n[0], n[1]);
+    constexpr int last = DIM - 1;
     const int KL = g.K[last], NL = g.N[last];
     const int B = g.B;
-    float s_lead = 1.f;
-    for (int d = 0; d < last; ++d) s_lead *= __ldg(g.sn[d] + n[d]);
+    const float s_lead = lead_sn<DIM>(g.sn[0], g.sn[1], n[0], n[1]);
     int64_t krow = inst;
+#pragma unroll
     for (int d = 0; d < last; ++d) krow = krow * g.K[d] + n[d];
     const float2* src = grid + (size_t)krow * KL * B;
-    const float2* ms = maps + (size_t)(r - inst * (g.prodN / NL)) * NL * B;
+    const float2* ms = maps + (size_t)r * NL * B;         // single-instance plans only
     float2* dst = x + (size_t)r * NL;
     for (int k = threadIdx.x; k < NL; k += blockDim.x) {
         float ax = 0.f, ay = 0.f;
@@ -255,8 +279,13 @@ static int row_threads(int len) {
 int launch_scale(const nufft_plan_s* p, const float2* in, float2* out, cudaStream_t s) {
     ImgGeom g = img_geom(p);
     const int64_t rows = rows_of(g, g.N, p->ninst);
-    scale_rows_kernel<<<row_blocks(p, rows), row_threads(g.N[g.ndim - 1] * g.B), 0, s>>>(g, in, out,
-                                                                                         rows);
+    const unsigned nb = row_blocks(p, rows);
+    const int nt = row_threads(g.N[g.ndim - 1] * g.B);
+    switch (p->ndim) {
+        case 1: scale_rows_kernel<1><<<nb, nt, 0, s>>>(g, in, out, rows); break;
+        case 2: scale_rows_kernel<2><<<nb, nt, 0, s>>>(g, in, out, rows); break;
+        default: scale_rows_kernel<3><<<nb, nt, 0, s>>>(g, in, out, rows); break;
+    }
     return check_launch("scale_rows_kernel");
 }
 
@@ -264,8 +293,14 @@ int launch_pad(const nufft_plan_s* p, const float2* xx, float2* grid, bool apply
                int dom_axis, cudaStream_t s) {
     ImgGeom g = img_geom(p);
     const int64_t rows = rows_of(g, g.K, p->ninst);
-    pad_rows_kernel<<<row_blocks(p, rows), row_threads(g.K[g.ndim - 1] * g.B), 0, s>>>(
-        g, xx, grid, apply_sn ? 1 : 0, dom_axis, rows);
+    const unsigned nb = row_blocks(p, rows);
+    const int nt = row_threads(g.K[g.ndim - 1] * g.B);
+    const int as = apply_sn ? 1 : 0;
+    switch (p->ndim) {
+        case 1: pad_rows_kernel<1><<<nb, nt, 0, s>>>(g, xx, grid, as, dom_axis, rows); break;
+        case 2: pad_rows_kernel<2><<<nb, nt, 0, s>>>(g, xx, grid, as, dom_axis, rows); break;
+        default: pad_rows_kernel<3><<<nb, nt, 0, s>>>(g, xx, grid, as, dom_axis, rows); break;
+    }
     return check_launch("pad_rows_kernel");
 }
 
@@ -274,8 +309,14 @@ int launch_crop(const nufft_plan_s* p, const float2* grid, float2* xx, bool appl
     ImgGeom g = img_geom(p);
     const float norm = (float)(1.0 / (double)p->prodK);
     const int64_t rows = rows_of(g, g.N, p->ninst);
-    crop_rows_kernel<<<row_blocks(p, rows), row_threads(g.N[g.ndim - 1] * g.B), 0, s>>>(
-        g, grid, xx, apply_sn ? 1 : 0, divide_sn ? 1 : 0, norm, rows);
+    const unsigned nb = row_blocks(p, rows);
+    const int nt = row_threads(g.N[g.ndim - 1] * g.B);
+    const int as = apply_sn ? 1 : 0, ds = divide_sn ? 1 : 0;
+    switch (p->ndim) {
+        case 1: crop_rows_kernel<1><<<nb, nt, 0, s>>>(g, grid, xx, as, ds, norm, rows); break;
+        case 2: crop_rows_kernel<2><<<nb, nt, 0, s>>>(g, grid, xx, as, ds, norm, rows); break;
+        default: crop_rows_kernel<3><<<nb, nt, 0, s>>>(g, grid, xx, as, ds, norm, rows); break;
+    }
     return check_launch("crop_rows_kernel");
 }
 
@@ -299,8 +340,13 @@ static int make_plan(cufftHandle* h, int rank, int* n, int stride, int dist, int
 int launch_pad_sense(const nufft_plan_s* p, const float2* x, float2* grid, cudaStream_t s) {
     ImgGeom g = img_geom(p);
     const int64_t rows = rows_of(g, g.K, p->ninst);
-    pad_sense_rows_kernel<<<row_blocks(p, rows), row_threads(g.K[g.ndim - 1] * g.B), 0, s>>>(
-        g, x, p->d_maps, grid, rows);
+    const unsigned nb = row_blocks(p, rows);
+    const int nt = row_threads(g.K[g.ndim - 1] * g.B);
+    switch (p->ndim) {
+        case 1: pad_sense_rows_kernel<1><<<nb, nt, 0, s>>>(g, x, p->d_maps, grid, rows); break;
+        case 2: pad_sense_rows_kernel<2><<<nb, nt, 0, s>>>(g, x, p->d_maps, grid, rows); break;
+        default: pad_sense_rows_kernel<3><<<nb, nt, 0, s>>>(g, x, p->d_maps, grid, rows); break;
+    }
     return check_launch("pad_sense_rows_kernel");
 }
 
@@ -308,8 +354,13 @@ int launch_crop_sense(const nufft_plan_s* p, const float2* grid, float2* x, cuda
     ImgGeom g = img_geom(p);
     const float norm = (float)(1.0 / (double)p->prodK);
     const int64_t rows = rows_of(g, g.N, p->ninst);
-    crop_sense_rows_kernel<<<row_blocks(p, rows), row_threads(g.N[g.ndim - 1]), 0, s>>>(
-        g, grid, p->d_maps, x, norm, rows);
+    const unsigned nb = row_blocks(p, rows);
+    const int nt = row_threads(g.N[g.ndim - 1]);
+    switch (p->ndim) {
+        case 1: crop_sense_rows_kernel<1><<<nb, nt, 0, s>>>(g, grid, p->d_maps, x, norm, rows); break;
+        case 2: crop_sense_rows_kernel<2><<<nb, nt, 0, s>>>(g, grid, p->d_maps, x, norm, rows); break;
+        default: crop_sense_rows_kernel<3><<<nb, nt, 0, s>>>(g, grid, p->d_maps, x, norm, rows); break;
+    }
     return check_launch("crop_sense_rows_kernel");
 }
 

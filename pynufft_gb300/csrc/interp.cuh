@@ -649,6 +649,112 @@ __global__ void __launch_bounds__(256) y2k_zteam_kernel(Geom g, const float2* __
 }
 
 // ---------------------------------------------------------------------------
+// y2k, one thread per point (B < 8): tile layout cell-major, coil fastest.
+// EX = every axis has exactly JM neighbours, so no loop guards are needed;
+// a single coil (the common case) addresses cells directly.
+// ---------------------------------------------------------------------------
+template <int DIM, int JM, bool EX, bool DET>
+__global__ void __launch_bounds__(128) y2k_point_kernel(Geom g, const float2* __restrict__ y,
+                                                        float2* __restrict__ grid,
+                                                        unsigned long long* __restrict__ igrid,
+                                                        int bc, const double* __restrict__ dscal) {
+    using T = typename Acc<DET>::T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float s_bound[8], s_scale[8];
+    const int4 sp = g.sub[blockIdx.x];
+    const int inst = sp.w;
+    int o[3];
+    tile_origin<DIM>(g, sp, o);
+    constexpr int DI = DIM - 1;
+    constexpr int DY = (DIM > 1) ? DIM - 2 : 0;
+    const int Tz = g.T[DI];
+    const int Ty = (DIM > 1) ? g.T[DY] : 1;
+    int ncell = 1;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
+    const int B = g.B;
+    const int J0 = EX ? JM : g.J[0];
+    const int Jy = EX ? JM : g.J[DY];
+    const int Jz = EX ? JM : g.J[DI];
+    T* tile = reinterpret_cast<T*>(smem_raw);
+
+    for (int b0 = 0; b0 < B; b0 += bc) {
+        const int bcur = min(bc, B - b0);
+        const int nsm = ncell * bcur;
+        for (int e = threadIdx.x; e < 2 * nsm; e += blockDim.x) tile[e] = 0;
+        if constexpr (DET) {
+            if (threadIdx.x < bcur) s_scale[threadIdx.x] = (float)dscal[1];
+            __syncthreads();
+        } else {
+            subproblem_scales(g, sp, y, b0, bcur, s_bound, s_scale);
+        }
+        T* re = tile;
+        T* im = tile + nsm;
+        for (int s = sp.y + threadIdx.x; s < sp.y + sp.z; s += blockDim.x) {
+            float2 cz[JM], cy[JM];
+            {
+                const float2* src = g.coef[DI] + (size_t)s * g.JP[DI];
+#pragma unroll
+                for (int k = 0; k < JM; ++k)
+                    cz[k] = (EX || k < Jz) ? __ldg(src + k) : make_float2(0.f, 0.f);
+            }
+            if constexpr (DIM > 1) {
+                const float2* src = g.coef[DY] + (size_t)s * g.JP[DY];
+#pragma unroll
+                for (int j = 0; j < JM; ++j)
+                    cy[j] = (EX || j < Jy) ? __ldg(src + j) : make_float2(0.f, 0.f);
+            }
+            const int lz = __ldg(g.pos[DI] + s) - o[DI];
+            const int ly = (DIM > 1) ? __ldg(g.pos[DY] + s) - o[DY] : 0;
+            const int lx = (DIM > 2) ? __ldg(g.pos[0] + s) - o[0] : 0;
+            const float2* c0src = g.coef[0] + (size_t)s * g.JP[0];
+            const int m = __ldg(g.perm + s);
+            for (int b = 0; b < bcur; ++b) {
+                const float sc = s_scale[b];
+                float2 yv = __ldg(y + (size_t)m * B + b0 + b);
+                yv.x *= sc;
+                yv.y *= sc;
+                const int ni = (DIM > 2) ? J0 : 1;
+#pragma unroll 1
+                for (int i = 0; i < ni; ++i) {
+                    const float2 wi = (DIM > 2) ? cmulc(yv, __ldg(c0src + i)) : yv;
+                    const int ci = (DIM > 2) ? (lx + i) * Ty : 0;
+#pragma unroll
+                    for (int j = 0; j < ((DIM > 1) ? JM : 1); ++j) {
+                        if (!EX && DIM > 1 && j >= Jy) continue;
+                        const float2 wij = (DIM > 1) ? cmulc(wi, cy[j]) : wi;
+                        const int cj = (DIM > 1) ? (ci + ly + j) * Tz + lz : lz;
+                        if (bcur == 1) {
+                            T* rr = re + cj;
+                            T* ii = im + cj;
+#pragma unroll
+                            for (int k = 0; k < JM; ++k) {
+                                if (!EX && k >= Jz) continue;
+                                const float2 w = cmulc(wij, cz[k]);
+                                atomicAdd(rr + k, Acc<DET>::fix(w.x, 1.f));
+                                atomicAdd(ii + k, Acc<DET>::fix(w.y, 1.f));
+                            }
+                        } else {
+#pragma unroll
+                            for (int k = 0; k < JM; ++k) {
+                                if (!EX && k >= Jz) continue;
+                                const float2 w = cmulc(wij, cz[k]);
+                                const int e = (cj + k) * bcur + b;
+                                atomicAdd(re + e, Acc<DET>::fix(w.x, 1.f));
+                                atomicAdd(im + e, Acc<DET>::fix(w.y, 1.f));
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        flush_tile<DIM, DET, true>(g, o, inst, ncell, b0, bcur, tile, s_scale, grid, igrid);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // y2k, coil-teams (B >= 8): tile layout cell-major, coil fastest
 // ---------------------------------------------------------------------------
 template <int DIM, int JM, int G, bool DET>

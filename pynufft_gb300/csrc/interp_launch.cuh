@@ -105,9 +105,16 @@ static int y2k_launch(const Geom& g, const float2* y, float2* grid, unsigned lon
         return NUFFT_EUNSUPPORTED;
     }
     void (*kern)(Geom, const float2*, float2*, unsigned long long*, int, const double*);
+    int threads = 256;
     if constexpr (G == 1) {
-        kern = (g.ymethod == NUFFT_Y2K_POINT) ? y2k_coil_kernel<DIM, JM, 1, DET>
-                                              : y2k_zteam_kernel<DIM, JM, DET>;
+        if (g.ymethod == NUFFT_Y2K_POINT) {
+            bool exact = true;
+            for (int d = 0; d < DIM; ++d) exact = exact && (g.J[d] == JM);
+            kern = exact ? y2k_point_kernel<DIM, JM, true, DET> : y2k_point_kernel<DIM, JM, false, DET>;
+            threads = 128;
+        } else {
+            kern = y2k_zteam_kernel<DIM, JM, DET>;
+        }
     } else {
         kern = y2k_coil_kernel<DIM, JM, G, DET>;
     }
@@ -119,7 +126,7 @@ static int y2k_launch(const Geom& g, const float2* y, float2* grid, unsigned lon
             return NUFFT_ECUDA;
         }
     }
-    if (g.nsub > 0) kern<<<(unsigned)g.nsub, 256, smem, s>>>(g, y, grid, igrid, bc, dscal);
+    if (g.nsub > 0) kern<<<(unsigned)g.nsub, threads, smem, s>>>(g, y, grid, igrid, bc, dscal);
     return check_launch("y2k_kernel");
 }
 

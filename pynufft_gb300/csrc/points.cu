@@ -28,6 +28,7 @@ namespace nufft {
 struct AxisTab {
     double cs[2 * NUFFT_MAXL + NUFFT_MAXJ + 2];  // cos(pi n N/K), n = -(L+J) .. L
     double ss[2 * NUFFT_MAXL + NUFFT_MAXJ + 2];  // sin(pi n N/K)
+    double rc[NUFFT_MAXJ], rs[NUFFT_MAXJ];       // cos, sin(gam (N-1)/2 j), j = 0..J-1
 };
 
 struct PointsArgs {
@@ -115,9 +116,13 @@ __device__ __forceinline__ double sinc_direct(double x) {
 //   c = T r                                                      (min_max)
 //   u_j = exp(i gam (N-1)/2 arg_j) c_j exp(-i om N/2)            (OMEGA_u)
 //   out_j = conj(u_j)                                            (.T.conj())
-// sin(pi (dk+n) N/K) for |dk+n| >= 1 uses the angle-sum identity with the
-// tabulated sin/cos(pi n N/K); the two terms nearest zero are evaluated
-// directly so the sinc keeps full relative accuracy near its peak.
+// The sinc argument is (dk + n) N/K with n = l - j, so only the 2L+J
+// distinct reciprocals 1/(dk + n) are computed, and sin(pi (dk+n) N/K) uses
+// the angle-sum identity with tabulated sin/cos(pi n N/K); the terms with
+// |dk + n| < 1 are evaluated directly so the sinc keeps full relative
+// accuracy near its peak.  The J phase factors come from one sincos rotated
+// by the tabulated exp(-i gam (N-1)/2 j).  This GPU's FP64 rate is low, so
+// divisions and transcendental calls are kept to a few per axis.
 __device__ float axis_coefs(const AxisConst& a, const AxisTab& tab, double w,
                             float2* __restrict__ out) {
     const int J = a.J, L = a.L;
@@ -126,31 +131,32 @@ __device__ float axis_coefs(const AxisConst& a, const AxisTab& tab, double w,
     double dk = t - koff;
     double s0, c0;
     sincospi(dk * a.inv_ratio, &s0, &c0);
+    // sinc values indexed by n + L + J, n = l - j in [-(L+J), L-1]
+    double sv[2 * NUFFT_MAXL + NUFFT_MAXJ + 2];
+    const double pr = M_PI * a.inv_ratio;
+    for (int n = -(L + J); n <= L - 1; ++n) {
+        const double xn = dk + n;
+        const int q = n + L + J;
+        sv[q] = (fabs(xn) < 1.0) ? sinc_direct(xn * a.inv_ratio)
+                                 : (s0 * tab.cs[q] + c0 * tab.ss[q]) / (pr * xn);
+    }
     double r[NUFFT_MAXJ];
     for (int j = 1; j <= J; ++j) {
         double acc = 0.0;
-        for (int l = -L; l <= L; ++l) {
-            double xn = dk - j + l;
-            double sv;
-            if (fabs(xn) < 1.0) {
-                sv = sinc_direct(xn * a.inv_ratio);
-            } else {
-                int n = l - j + L + J;
-                double sn = s0 * tab.cs[n] + c0 * tab.ss[n];
-                sv = sn / (M_PI * xn * a.inv_ratio);
-            }
-            acc += a.alpha[l < 0 ? -l : l] * sv;
-        }
+        for (int l = -L; l <= L; ++l) acc += a.alpha[l < 0 ? -l : l] * sv[l - j + L + J];
         r[j - 1] = acc;
     }
+    // phase of j = 1: lin*(dk - 1) - om*N/2; then rotate by exp(-i lin) per step
+    double sth, cth;
+    sincos(a.lin * (dk - 1.0) - w * a.half_N, &sth, &cth);
     float amax = 0.f;
     for (int j = 0; j < J; ++j) {
         double c = 0.0;
         for (int i = 0; i < J; ++i) c += a.T[j * J + i] * r[i];
-        double th = a.lin * (dk - (j + 1)) - w * a.half_N;
-        double sth, cth;
-        sincos(th, &sth, &cth);
-        float2 v = make_float2((float)(c * cth), (float)(-c * sth));
+        // exp(i th_j) with th_j = th_1 - lin*j
+        const double cr = cth * tab.rc[j] + sth * tab.rs[j];
+        const double ci = sth * tab.rc[j] - cth * tab.rs[j];
+        float2 v = make_float2((float)(c * cr), (float)(-c * ci));
         out[j] = v;
         amax = fmaxf(amax, sqrtf(v.x * v.x + v.y * v.y));
     }
@@ -349,6 +355,10 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
             double ang = M_PI * n * a.inv_ratio;
             htab[d].cs[n + ap.L + ap.J] = std::cos(ang);
             htab[d].ss[n + ap.L + ap.J] = std::sin(ang);
+        }
+        for (int j = 0; j < ap.J; ++j) {
+            htab[d].rc[j] = std::cos(a.lin * j);
+            htab[d].rs[j] = std::sin(a.lin * j);
         }
     }
     AxisTab* d_tab = nullptr;
