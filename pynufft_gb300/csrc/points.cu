@@ -48,14 +48,19 @@ __device__ __forceinline__ int inst_of(const int64_t* start, int ninst, int64_t 
 // Step 1: bins.  koff = floor(om/gam - J/2) (nufft_offset, helper.py:900-907);
 // the footprint along an axis is (koff + j) mod K, j = 1..J (OMEGA_k,
 // helper.py:164-210), so its first index is pos = (koff + 1) mod K.
+// Within a bin, points are further keyed by the shared-memory bank of their
+// footprint origin in the gridding tile (cell index mod 32); step 3 deals
+// the keys round-robin so the 32 points that share a warp start in distinct
+// banks wherever the bin allows it.
 __global__ void bin_points_kernel(const double* __restrict__ om, int64_t M, int ndim,
                                   const AxisConst* __restrict__ axc, Geom g,
                                   int* __restrict__ bin_of, int* __restrict__ rank_of,
-                                  int* __restrict__ bin_count, int* __restrict__ err) {
+                                  int* __restrict__ bucket_count, int* __restrict__ err) {
     for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
          m += (int64_t)gridDim.x * blockDim.x) {
         int inst = (g.ninst > 1) ? inst_of(g.inst_start, g.ninst, m) : 0;
         int64_t bin = 0;
+        int cell = 0;
         bool ok = true;
         for (int d = 0; d < ndim; ++d) {
             double w = om[m * ndim + d];
@@ -68,7 +73,9 @@ __global__ void bin_points_kernel(const double* __restrict__ om, int64_t M, int 
             int pos = (int)r;
             if (pos >= a.K) pos -= a.K;
             if (pos < 0) pos += a.K;
-            bin = bin * g.nb[d] + pos / g.bs[d];
+            const int b = pos / g.bs[d];
+            bin = bin * g.nb[d] + b;
+            cell = cell * g.T[d] + (pos - b * g.bs[d]);
         }
         if (!ok) {
             atomicOr(err, 1);
@@ -76,8 +83,19 @@ __global__ void bin_points_kernel(const double* __restrict__ om, int64_t M, int 
             continue;
         }
         bin += (int64_t)inst * g.nbin_inst;
-        bin_of[m] = (int)bin;
-        rank_of[m] = atomicAdd(&bin_count[bin], 1);
+        bin_of[m] = (int)(bin * 32 + (cell & 31));
+        rank_of[m] = atomicAdd(&bucket_count[bin * 32 + (cell & 31)], 1);
+    }
+}
+
+// Points per bin from the 32 bank buckets of each bin.
+__global__ void bin_totals_kernel(const int* __restrict__ bucket_count, int64_t nbins,
+                                  int* __restrict__ bin_count) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbins;
+         b += (int64_t)gridDim.x * blockDim.x) {
+        int t = 0;
+        for (int k = 0; k < 32; ++k) t += bucket_count[b * 32 + k];
+        bin_count[b] = t;
     }
 }
 
@@ -169,6 +187,7 @@ __global__ void build_tables_kernel(const double* __restrict__ om, int64_t M, in
                                     const int* __restrict__ bin_of,
                                     const int* __restrict__ rank_of,
                                     const int* __restrict__ bin_start,
+                                    const int* __restrict__ bucket_count,
                                     int* __restrict__ perm, int* __restrict__ pos,
                                     float2* __restrict__ coef0, float2* __restrict__ coef1,
                                     float2* __restrict__ coef2, float* __restrict__ wpt,
@@ -176,9 +195,18 @@ __global__ void build_tables_kernel(const double* __restrict__ om, int64_t M, in
     float2* coefs[3] = {coef0, coef1, coef2};
     for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
          m += (int64_t)gridDim.x * blockDim.x) {
-        int bin = bin_of[m];
-        if (bin < 0) continue;
-        int64_t s = (int64_t)bin_start[bin] + rank_of[m];
+        const int bk = bin_of[m];
+        if (bk < 0) continue;
+        const int bin = bk >> 5, key = bk & 31, rank = rank_of[m];
+        // position in the round-robin deal over the bin's 32 bank buckets:
+        // all elements of earlier rounds, then earlier buckets of this round
+        const int* c = bucket_count + (int64_t)bin * 32;
+        int off = 0;
+        for (int k = 0; k < 32; ++k) {
+            const int ck = c[k];
+            off += min(ck, rank) + ((k < key && ck > rank) ? 1 : 0);
+        }
+        int64_t s = (int64_t)bin_start[bin] + off;
         perm[s] = (int)m;
         float wprod = 1.f;
         for (int d = 0; d < ndim; ++d) {
@@ -303,12 +331,13 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     // temporaries
     double* d_om = nullptr;
     int *d_bin_of = nullptr, *d_rank = nullptr, *d_cnt = nullptr, *d_start = nullptr;
-    int *d_nsub = nullptr, *d_subst = nullptr, *d_err = nullptr;
+    int *d_nsub = nullptr, *d_subst = nullptr, *d_err = nullptr, *d_bucket = nullptr;
     unsigned int* d_wmax = nullptr;
     auto cleanup = [&]() {
         if (!om_on_device) cudaFree(d_om);
         cudaFree(d_bin_of); cudaFree(d_rank); cudaFree(d_cnt); cudaFree(d_start);
         cudaFree(d_nsub); cudaFree(d_subst); cudaFree(d_err); cudaFree(d_wmax);
+        cudaFree(d_bucket);
     };
 #define TRY_TMP(expr)                                                              \
     do {                                                                           \
@@ -329,12 +358,13 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     TRY_TMP(cudaMalloc(&d_bin_of, sizeof(int) * Malloc));
     TRY_TMP(cudaMalloc(&d_rank, sizeof(int) * Malloc));
     TRY_TMP(cudaMalloc(&d_cnt, sizeof(int) * nbins));
+    TRY_TMP(cudaMalloc(&d_bucket, sizeof(int) * nbins * 32));
     TRY_TMP(cudaMalloc(&d_start, sizeof(int) * (nbins + 1)));
     TRY_TMP(cudaMalloc(&d_nsub, sizeof(int) * nbins));
     TRY_TMP(cudaMalloc(&d_subst, sizeof(int) * (nbins + 1)));
     TRY_TMP(cudaMalloc(&d_err, sizeof(int)));
     TRY_TMP(cudaMalloc(&d_wmax, sizeof(unsigned int)));
-    TRY_TMP(cudaMemsetAsync(d_cnt, 0, sizeof(int) * nbins, s));
+    TRY_TMP(cudaMemsetAsync(d_bucket, 0, sizeof(int) * nbins * 32, s));
     TRY_TMP(cudaMemsetAsync(d_err, 0, sizeof(int), s));
     TRY_TMP(cudaMemsetAsync(d_wmax, 0, sizeof(unsigned int), s));
 
@@ -372,7 +402,12 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     const int blocks = (int)std::min<int64_t>((M + threads - 1) / threads + 1, 65535 * 8);
     if (M > 0) {
         bin_points_kernel<<<blocks, threads, 0, s>>>(d_om, M, nd, p->d_axc, g, d_bin_of, d_rank,
-                                                     d_cnt, d_err);
+                                                     d_bucket, d_err);
+        TRY_TMP(cudaGetLastError());
+    }
+    {
+        const int tb = (int)std::min<int64_t>((nbins + threads - 1) / threads, 65535);
+        bin_totals_kernel<<<tb, threads, 0, s>>>(d_bucket, nbins, d_cnt);
         TRY_TMP(cudaGetLastError());
     }
     scan_kernel<<<1, 1024, 0, s>>>(d_cnt, d_start, nbins);
@@ -382,7 +417,7 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     float2* c2 = c1 + (nd > 2 ? Malloc * JP[1] : 0);
     if (M > 0) {
         build_tables_kernel<<<blocks, threads, 0, s>>>(d_om, M, nd, p->d_axc, d_tab, g, d_bin_of,
-                                                       d_rank, d_start, p->d_perm, p->d_pos,
+                                                       d_rank, d_start, d_bucket, p->d_perm, p->d_pos,
                                                        c0, c1, c2, p->d_wpt, d_wmax);
         TRY_TMP(cudaGetLastError());
     }
