@@ -104,6 +104,8 @@ int nufft_plan_set_bins(nufft_plan_t plan, const int* bin_shape, int max_sub_poi
 #define NUFFT_K2Y_ZTEAM 1   /* J lanes per point along the innermost axis     */
 #define NUFFT_K2Y_POINT 2   /* one thread per point                           */
 #define NUFFT_K2Y_TILE  3   /* bin footprint staged in shared memory + z-teams */
+#define NUFFT_K2Y_TILE_POINT 4  /* bin footprint in shared memory + 1-2 threads
+                                   per point                                   */
 #define NUFFT_Y2K_COIL  0   /* (internal) lanes over coils                    */
 #define NUFFT_Y2K_ZTEAM 1   /* J lanes per point along the innermost axis     */
 #define NUFFT_Y2K_POINT 2   /* one thread per point                           */

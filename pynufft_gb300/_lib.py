@@ -23,7 +23,7 @@ NUFFT_ENOPOINTS = 6
 NUFFT_ECG_BREAKDOWN = 7
 NUFFT_EUNSUPPORTED = 8
 NUFFT_FLAG_DETERMINISTIC = 1
-NUFFT_K2Y_ZTEAM, NUFFT_K2Y_POINT, NUFFT_K2Y_TILE = 1, 2, 3
+NUFFT_K2Y_ZTEAM, NUFFT_K2Y_POINT, NUFFT_K2Y_TILE, NUFFT_K2Y_TILE_POINT = 1, 2, 3, 4
 NUFFT_Y2K_ZTEAM, NUFFT_Y2K_POINT, NUFFT_Y2K_GLOBAL = 1, 2, 3
 
 # every symbol the header declares, with (restype, argtypes)

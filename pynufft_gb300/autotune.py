@@ -26,7 +26,7 @@ BIN_CANDIDATES = {
     3: [(4, 8, 8), (8, 8, 8), (8, 8, 16), (16, 16, 16)],
 }
 SUB_CANDIDATES = [128, 256, 512]
-K2Y = ['tile', 'zteam', 'point']
+K2Y = ['tile', 'tile_point', 'zteam', 'point']
 Y2K = ['zteam', 'point', 'global']
 
 

@@ -47,10 +47,14 @@ nufft::Geom nufft_plan_s::geom() const {
     g.wpt = d_wpt;
     g.sub = d_sub;
     g.nsub = nsub;
-    // lane mappings: coil-teams for B >= 8; otherwise the plan's choice, with
-    // one thread per point as the default for both (fastest in measurement
-    // on 2D radial and 3D uniform trajectories; the autotuner may pick others)
-    g.kmethod = (B >= 8) ? NUFFT_K2Y_COIL : (k2y_method ? k2y_method : NUFFT_K2Y_POINT);
+    // lane mappings: coil-teams for B >= 8; otherwise the plan's choice.  The
+    // defaults (fastest in measurement on 2D radial and 3D uniform
+    // trajectories; the autotuner may pick others): k2y gathers from a shared
+    // tile when sub-problems hold 8 or more points on average (the tile load
+    // is then shared by enough points), else straight from the grid; y2k one
+    // thread per point.
+    const int kdef = (nsub > 0 && M >= 8 * (int64_t)nsub) ? NUFFT_K2Y_TILE_POINT : NUFFT_K2Y_POINT;
+    g.kmethod = (B >= 8) ? NUFFT_K2Y_COIL : (k2y_method ? k2y_method : kdef);
     g.ymethod = (B >= 8) ? NUFFT_Y2K_COIL : (y2k_method ? y2k_method : NUFFT_Y2K_POINT);
     // the exact mode's 64-bit atomics favour the z-team mapping (fewer bank
     // conflicts); it has no global-atomic variant
@@ -236,7 +240,7 @@ int nufft_plan_set_bins(nufft_plan_t p, const int* bin_shape, int max_sub_points
 
 int nufft_plan_set_methods(nufft_plan_t p, int k2y_method, int y2k_method) {
     NUFFT_TRY(need_plan(p, "nufft_plan_set_methods"));
-    if (k2y_method < 0 || k2y_method > NUFFT_K2Y_TILE || y2k_method < 0 ||
+    if (k2y_method < 0 || k2y_method > NUFFT_K2Y_TILE_POINT || y2k_method < 0 ||
         y2k_method > NUFFT_Y2K_GLOBAL) {
         set_error("nufft_plan_set_methods: unknown method");
         return NUFFT_EINVAL;

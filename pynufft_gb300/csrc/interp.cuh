@@ -481,6 +481,124 @@ __global__ void __launch_bounds__(256) k2y_tile_kernel(Geom g, const float2* __r
 }
 
 // ---------------------------------------------------------------------------
+// Paired-thread kernels (B == 1 gridding, B < 8 interpolation): the block
+// stages the sub-problem's footprint in shared memory in the padded layout
+// of tile_strides; in 2D/3D each point is served by two threads 16 lanes
+// apart that take alternate taps of the outer axis (x in 3D, y in 2D).  A
+// warp thus holds 16 points; the bank-aware point order gives them distinct
+// padded addresses mod 16, and the padding puts a point's second thread 16
+// banks from its first, so a warp's 32 accesses of one tap fall in 32
+// distinct banks whenever the bin's keys allow it.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__device__ __forceinline__ int tile_addr(const int (&t)[3], const TileStrides& ts) {
+    if constexpr (DIM == 3) return t[0] * ts.sx + t[1] * ts.sy + t[2];
+    else if constexpr (DIM == 2) return t[0] * ts.sy + t[1];
+    else return t[0];
+}
+
+// k2y from the shared tile.  EX: every axis has exactly JM taps.
+template <int DIM, int JM, bool EX>
+__global__ void __launch_bounds__(128) k2y_spoint_kernel(Geom g, const float2* __restrict__ grid,
+                                                         float2* __restrict__ y) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* tile = reinterpret_cast<float2*>(smem_raw);
+    const int4 sp = g.sub[blockIdx.x];
+    int o[3];
+    tile_origin<DIM>(g, sp, o);
+    constexpr int DI = DIM - 1;
+    constexpr int DY = (DIM > 1) ? DIM - 2 : 0;
+    constexpr int P = (DIM > 1) ? 2 : 1;   // threads per point
+    constexpr int PW = 32 / P;             // points per warp
+    const TileStrides ts = tile_strides(DIM, g.T);
+    int ncell = 1;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
+    const int B = g.B;
+    const int J0 = EX ? JM : g.J[0];
+    const int Jy = EX ? JM : g.J[DY];
+    const int Jz = EX ? JM : g.J[DI];
+    const size_t ibase = (size_t)sp.w * g.prodK;
+    const int lane = threadIdx.x & 31;
+    const int q = lane / PW;
+    const int pw = lane - q * PW;
+    const int per_round = (int)(blockDim.x >> 5) * PW;
+    const int end = sp.y + sp.z;
+
+    for (int b = 0; b < B; ++b) {
+        TileWalk<DIM> w;
+        w.init(g.T, threadIdx.x, blockDim.x);
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x, w.next())
+            tile[tile_addr<DIM>(w.t, ts)] = __ldg(grid + (ibase + w.cell(g, o)) * B + b);
+        __syncthreads();
+        for (int base_s = sp.y; base_s < end; base_s += per_round) {
+            const int s = base_s + (int)(threadIdx.x >> 5) * PW + pw;
+            const bool active = s < end;
+            float2 acc = make_float2(0.f, 0.f);
+            if (active) {
+                const int lz = __ldg(g.pos[DI] + s) - o[DI];
+                float2 cz[JM];
+                {
+                    const float2* src = g.coef[DI] + (size_t)s * g.JP[DI];
+#pragma unroll
+                    for (int k = 0; k < JM; ++k)
+                        cz[k] = (EX || k < Jz) ? __ldg(src + k) : make_float2(0.f, 0.f);
+                }
+                if constexpr (DIM == 1) {
+#pragma unroll
+                    for (int k = 0; k < JM; ++k)
+                        if (EX || k < Jz) cfma(acc, cz[k], tile[lz + k]);
+                } else if constexpr (DIM == 2) {
+                    const int ly = __ldg(g.pos[DY] + s) - o[DY];
+                    const float2* csrc = g.coef[DY] + (size_t)s * g.JP[DY];
+#pragma unroll 1
+                    for (int j = q; j < Jy; j += P) {
+                        const float2* row = tile + (ly + j) * ts.sy + lz;
+                        float2 r = make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int k = 0; k < JM; ++k)
+                            if (EX || k < Jz) cfma(r, cz[k], row[k]);
+                        cfma(acc, __ldg(csrc + j), r);
+                    }
+                } else {
+                    const int ly = __ldg(g.pos[DY] + s) - o[DY];
+                    const int lx = __ldg(g.pos[0] + s) - o[0];
+                    float2 cy[JM];
+                    {
+                        const float2* src = g.coef[DY] + (size_t)s * g.JP[DY];
+#pragma unroll
+                        for (int j = 0; j < JM; ++j)
+                            cy[j] = (EX || j < Jy) ? __ldg(src + j) : make_float2(0.f, 0.f);
+                    }
+                    const float2* c0src = g.coef[0] + (size_t)s * g.JP[0];
+#pragma unroll 1
+                    for (int i = q; i < J0; i += P) {
+                        const float2* pl = tile + (lx + i) * ts.sx + ly * ts.sy + lz;
+                        float2 t = make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int j = 0; j < JM; ++j) {
+                            if (!EX && j >= Jy) continue;
+                            float2 r = make_float2(0.f, 0.f);
+#pragma unroll
+                            for (int k = 0; k < JM; ++k)
+                                if (EX || k < Jz) cfma(r, cz[k], pl[j * ts.sy + k]);
+                            cfma(t, cy[j], r);
+                        }
+                        cfma(acc, __ldg(c0src + i), t);
+                    }
+                }
+            }
+            if constexpr (P == 2) {
+                acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 16);
+                acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 16);
+            }
+            if (active && q == 0) y[(size_t)__ldg(g.perm + s) * B + b] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // y2k shared pieces
 // ---------------------------------------------------------------------------
 // Fixed-point accumulator types: 32-bit with a per-sub-problem scale (fast
@@ -751,6 +869,108 @@ __global__ void __launch_bounds__(128) y2k_point_kernel(Geom g, const float2* __
         __syncthreads();
         flush_tile<DIM, DET, true>(g, o, inst, ncell, b0, bcur, tile, s_scale, grid, igrid);
         __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// y2k, paired threads per point (B == 1, 2D/3D, fast mode): 32-bit
+// fixed-point tile in the padded layout of tile_strides (re plane, then im
+// plane), flushed with float2 atomics.  EX: every axis has exactly JM taps.
+// (Multiplying the innermost axis in integers, to save the float-to-integer
+// conversions, measured slower than converting each tap.)
+// ---------------------------------------------------------------------------
+template <int JM>
+__device__ __forceinline__ void add_row(unsigned* re, unsigned* im, int c, float2 u,
+                                        const float2 (&cz)[JM], int Jz, bool ex) {
+#pragma unroll
+    for (int k = 0; k < JM; ++k) {
+        if (!ex && k >= Jz) continue;
+        const float2 w = cmulc(u, cz[k]);
+        atomicAdd(re + c + k, Acc<false>::fix(w.x, 1.f));
+        atomicAdd(im + c + k, Acc<false>::fix(w.y, 1.f));
+    }
+}
+
+template <int DIM, int JM, bool EX>
+__global__ void __launch_bounds__(128) y2k_spoint_kernel(Geom g, const float2* __restrict__ y,
+                                                         float2* __restrict__ grid) {
+    static_assert(DIM > 1, "paired gridding splits an outer axis");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float s_bound[1], s_scale[1];
+    const int4 sp = g.sub[blockIdx.x];
+    int o[3];
+    tile_origin<DIM>(g, sp, o);
+    constexpr int DI = DIM - 1;
+    constexpr int DY = DIM - 2;
+    const TileStrides ts = tile_strides(DIM, g.T);
+    const int J0 = EX ? JM : g.J[0];
+    const int Jy = EX ? JM : g.J[DY];
+    const int Jz = EX ? JM : g.J[DI];
+    unsigned* re = reinterpret_cast<unsigned*>(smem_raw);
+    unsigned* im = re + ts.n;
+    for (int e = threadIdx.x; e < 2 * ts.n; e += blockDim.x) re[e] = 0u;
+    subproblem_scales(g, sp, y, 0, 1, s_bound, s_scale);   // ends with a barrier
+    const float sc = s_scale[0];
+    const int lane = threadIdx.x & 31;
+    const int q = lane >> 4, pw = lane & 15;
+    const int per_round = (int)(blockDim.x >> 5) * 16;
+    const int end = sp.y + sp.z;
+    for (int base_s = sp.y; base_s < end; base_s += per_round) {
+        const int s = base_s + (int)(threadIdx.x >> 5) * 16 + pw;
+        if (s >= end) continue;
+        float2 cz[JM];
+        {
+            const float2* src = g.coef[DI] + (size_t)s * g.JP[DI];
+#pragma unroll
+            for (int k = 0; k < JM; ++k)
+                cz[k] = (EX || k < Jz) ? __ldg(src + k) : make_float2(0.f, 0.f);
+        }
+        const int lz = __ldg(g.pos[DI] + s) - o[DI];
+        const int ly = __ldg(g.pos[DY] + s) - o[DY];
+        float2 yv = __ldg(y + __ldg(g.perm + s));
+        yv.x *= sc;
+        yv.y *= sc;
+        if constexpr (DIM == 2) {
+            const float2* csrc = g.coef[DY] + (size_t)s * g.JP[DY];
+#pragma unroll 1
+            for (int j = q; j < Jy; j += 2)
+                add_row<JM>(re, im, (ly + j) * ts.sy + lz, cmulc(yv, __ldg(csrc + j)), cz, Jz, EX);
+        } else {
+            const int lx = __ldg(g.pos[0] + s) - o[0];
+            float2 cy[JM];
+            {
+                const float2* src = g.coef[DY] + (size_t)s * g.JP[DY];
+#pragma unroll
+                for (int j = 0; j < JM; ++j)
+                    cy[j] = (EX || j < Jy) ? __ldg(src + j) : make_float2(0.f, 0.f);
+            }
+            const float2* c0src = g.coef[0] + (size_t)s * g.JP[0];
+#pragma unroll 1
+            for (int i = q; i < J0; i += 2) {
+                const float2 wi = cmulc(yv, __ldg(c0src + i));
+                const int ci = (lx + i) * ts.sx + ly * ts.sy + lz;
+#pragma unroll
+                for (int j = 0; j < JM; ++j) {
+                    if (!EX && j >= Jy) continue;
+                    add_row<JM>(re, im, ci + j * ts.sy, cmulc(wi, cy[j]), cz, Jz, EX);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    int ncell = 1;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
+    const float inv = 1.f / sc;
+    const size_t ibase = (size_t)sp.w * g.prodK;
+    TileWalk<DIM> w;
+    w.init(g.T, threadIdx.x, blockDim.x);
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x, w.next()) {
+        const int a = tile_addr<DIM>(w.t, ts);
+        const unsigned vx = re[a], vy = im[a];
+        if (vx == 0u && vy == 0u) continue;
+        atomicAdd(grid + ibase + w.cell(g, o),
+                  make_float2(__int2float_rn((int)vx) * inv, __int2float_rn((int)vy) * inv));
     }
 }
 

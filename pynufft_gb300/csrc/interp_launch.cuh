@@ -22,16 +22,25 @@ template <int DIM, int JM, int G>
 static void k2y_launch(const Geom& g, const float2* grid, float2* y, cudaStream_t s) {
     const int threads = 256;
     if constexpr (G == 1) {
-        if (g.kmethod == NUFFT_K2Y_TILE) {
-            int ncell = 1;
-            for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
-            const size_t smem = sizeof(float2) * ncell;
+        int ncell = 1;
+        for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
+        const bool paired = g.kmethod == NUFFT_K2Y_TILE_POINT;
+        const size_t smem = sizeof(float2) * (paired ? tile_strides(DIM, g.T).n : ncell);
+        // a footprint beyond 200 KB of shared memory gathers from the grid
+        const bool tiled = (g.kmethod == NUFFT_K2Y_TILE || paired);
+        if (tiled && smem <= 200 * 1024) {
+            void (*kern)(Geom, const float2*, float2*) = k2y_tile_kernel<DIM, JM>;
+            int nt = threads;
+            if (paired) {
+                bool exact = true;
+                for (int d = 0; d < DIM; ++d) exact = exact && (g.J[d] == JM);
+                kern = exact ? k2y_spoint_kernel<DIM, JM, true> : k2y_spoint_kernel<DIM, JM, false>;
+                nt = 128;
+            }
             if (smem > 48 * 1024)
-                cudaFuncSetAttribute(k2y_tile_kernel<DIM, JM>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (g.nsub > 0)
-                k2y_tile_kernel<DIM, JM><<<(unsigned)g.nsub, threads, smem, s>>>(g, grid, y);
-        } else if (g.kmethod == NUFFT_K2Y_POINT) {
+                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (g.nsub > 0) kern<<<(unsigned)g.nsub, nt, smem, s>>>(g, grid, y);
+        } else if (g.kmethod == NUFFT_K2Y_POINT || tiled) {
             const int64_t blocks = (g.M + threads - 1) / threads;
             if (g.B == 1)
                 k2y_point_kernel<DIM, JM><<<(unsigned)blocks, threads, 0, s>>>(g, grid, y);
@@ -103,6 +112,26 @@ static int y2k_launch(const Geom& g, const float2* y, float2* grid, unsigned lon
     if (bc == 0) {
         set_error("y2k: gridding tile does not fit in shared memory; use a smaller bin shape");
         return NUFFT_EUNSUPPORTED;
+    }
+    if constexpr (G == 1 && !DET && DIM > 1) {
+        // one coil: paired threads per point on the padded tile
+        const size_t psmem = 2 * sizeof(unsigned) * tile_strides(DIM, g.T).n;
+        if (g.ymethod == NUFFT_Y2K_POINT && g.B == 1 && psmem <= 200 * 1024) {
+            bool exact = true;
+            for (int d = 0; d < DIM; ++d) exact = exact && (g.J[d] == JM);
+            void (*pk)(Geom, const float2*, float2*) =
+                exact ? y2k_spoint_kernel<DIM, JM, true> : y2k_spoint_kernel<DIM, JM, false>;
+            if (psmem > 48 * 1024) {
+                cudaError_t e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)psmem);
+                if (e != cudaSuccess) {
+                    set_error(std::string("y2k: cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+                    return NUFFT_ECUDA;
+                }
+            }
+            if (g.nsub > 0) pk<<<(unsigned)g.nsub, 128, psmem, s>>>(g, y, grid);
+            return check_launch("y2k_spoint_kernel");
+        }
     }
     void (*kern)(Geom, const float2*, float2*, unsigned long long*, int, const double*);
     int threads = 256;

@@ -61,6 +61,32 @@ struct Geom {
     int ymethod;                 // y2k lane mapping (NUFFT_Y2K_*), resolved
 };
 
+// Padded shared-tile layout of the paired-thread kernels: tile cell
+// (x, y, z) (z fastest; tile extents T) sits at word x*sx + y*sy + z.  The
+// stride of the axis whose taps the two threads of a point split (x in 3D,
+// y in 2D) is padded to 16 mod 32, so the two threads of a point always
+// address words 16 banks apart; n is the padded cell count.
+struct TileStrides {
+    int sy, sx, n;
+};
+__host__ __device__ inline int pad_to_16_mod_32(int v) { return v + ((16 - v % 32) + 32) % 32; }
+__host__ __device__ inline TileStrides tile_strides(int ndim, const int* T) {
+    TileStrides s{0, 0, T[0]};
+    if (ndim == 2) {
+        s.sy = pad_to_16_mod_32(T[1]);
+        s.n = T[0] * s.sy;
+    } else if (ndim == 3) {
+        s.sy = T[2];
+        s.sx = pad_to_16_mod_32(T[1] * T[2]);
+        s.n = T[0] * s.sx;
+    }
+    return s;
+}
+// Bank buckets per bin used to order the points of a bin: 16 residues of the
+// padded address in 2D/3D (a warp holds 16 points, each split over two
+// threads 16 banks apart), 32 in 1D (a warp holds 32 points).
+__host__ __device__ inline int bank_keys(int ndim) { return ndim == 1 ? 32 : 16; }
+
 }  // namespace nufft
 
 struct nufft_plan_s {

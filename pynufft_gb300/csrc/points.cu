@@ -49,9 +49,9 @@ __device__ __forceinline__ int inst_of(const int64_t* start, int ninst, int64_t 
 // the footprint along an axis is (koff + j) mod K, j = 1..J (OMEGA_k,
 // helper.py:164-210), so its first index is pos = (koff + 1) mod K.
 // Within a bin, points are further keyed by the shared-memory bank of their
-// footprint origin in the gridding tile (cell index mod 32); step 3 deals
-// the keys round-robin so the 32 points that share a warp start in distinct
-// banks wherever the bin allows it.
+// footprint origin in the padded tile layout (tile_strides; address mod 16
+// in 2D/3D, mod 32 in 1D); step 3 deals the keys round-robin so the points
+// that share a warp start in distinct banks wherever the bin allows it.
 __global__ void bin_points_kernel(const double* __restrict__ om, int64_t M, int ndim,
                                   const AxisConst* __restrict__ axc, Geom g,
                                   int* __restrict__ bin_of, int* __restrict__ rank_of,
@@ -60,7 +60,7 @@ __global__ void bin_points_kernel(const double* __restrict__ om, int64_t M, int 
          m += (int64_t)gridDim.x * blockDim.x) {
         int inst = (g.ninst > 1) ? inst_of(g.inst_start, g.ninst, m) : 0;
         int64_t bin = 0;
-        int cell = 0;
+        int lp[3] = {0, 0, 0};
         bool ok = true;
         for (int d = 0; d < ndim; ++d) {
             double w = om[m * ndim + d];
@@ -75,7 +75,7 @@ __global__ void bin_points_kernel(const double* __restrict__ om, int64_t M, int 
             if (pos < 0) pos += a.K;
             const int b = pos / g.bs[d];
             bin = bin * g.nb[d] + b;
-            cell = cell * g.T[d] + (pos - b * g.bs[d]);
+            lp[d] = pos - b * g.bs[d];
         }
         if (!ok) {
             atomicOr(err, 1);
@@ -83,8 +83,14 @@ __global__ void bin_points_kernel(const double* __restrict__ om, int64_t M, int 
             continue;
         }
         bin += (int64_t)inst * g.nbin_inst;
-        bin_of[m] = (int)(bin * 32 + (cell & 31));
-        rank_of[m] = atomicAdd(&bucket_count[bin * 32 + (cell & 31)], 1);
+        // bank key: the point's first footprint cell in the padded tile
+        // layout, modulo the bank buckets of the dimension
+        const TileStrides ts = tile_strides(ndim, g.T);
+        const int addr = (ndim == 3) ? lp[0] * ts.sx + lp[1] * ts.sy + lp[2]
+                         : (ndim == 2) ? lp[0] * ts.sy + lp[1] : lp[0];
+        const int key = addr & (bank_keys(ndim) - 1);
+        bin_of[m] = (int)(bin * 32 + key);
+        rank_of[m] = atomicAdd(&bucket_count[bin * 32 + key], 1);
     }
 }
 

@@ -220,12 +220,12 @@ class NUFFT:
         except Exception:
             pass
 
-    K2Y_METHODS = {'zteam': 1, 'point': 2, 'tile': 3}
+    K2Y_METHODS = {'zteam': 1, 'point': 2, 'tile': 3, 'tile_point': 4}
     Y2K_METHODS = {'zteam': 1, 'point': 2, 'global': 3}
 
     def set_methods(self, k2y=None, y2k=None):
         """Choose the lane mapping of the interpolation/gridding kernels for
-        plans with fewer than 8 coils: k2y in {'tile', 'zteam', 'point'},
+        plans with fewer than 8 coils: k2y in {'tile', 'tile_point', 'zteam', 'point'},
         y2k in {'zteam', 'point', 'global'}; None keeps the default."""
         km = 0 if k2y is None else self.K2Y_METHODS[k2y]
         ym = 0 if y2k is None else self.Y2K_METHODS[y2k]

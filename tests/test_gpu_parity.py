@@ -278,7 +278,8 @@ def test_full_size_3d_against_exact_nudft(NUFFT):
 
 
 @pytest.mark.parametrize('case', ['plan_1d', 'plan_2d', 'plan_3d', 'plan_3d_aniso', 'plan_2d_J8'])
-@pytest.mark.parametrize('k2y,y2k', [('tile', 'zteam'), ('zteam', 'point'), ('point', 'global')])
+@pytest.mark.parametrize('k2y,y2k', [('tile', 'zteam'), ('zteam', 'point'), ('point', 'global'),
+                                     ('tile_point', 'point')])
 def test_every_lane_mapping_matches_reference(NUFFT, case, k2y, y2k):
     g = load_golden(case)
     A = NUFFT(0)
