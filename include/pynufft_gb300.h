@@ -98,8 +98,11 @@ int nufft_plan_set_bins(nufft_plan_t plan, const int* bin_shape, int max_sub_poi
 
 /* Lane mappings of the interpolation (k2y) and gridding (y2k) kernels for
  * plans with fewer than 8 coils (plans with 8 or more always split coils
- * across lanes).  0 keeps the default (one thread per point).  Used by the
- * autotuner; results are identical up to float32 rounding order. */
+ * across lanes).  0 keeps the default: k2y gathers from a shared tile with two
+ * threads per point when sub-problems average 8 or more points (else one
+ * thread per point straight from the grid); y2k uses one thread per point
+ * (two for single-coil 2D/3D plans).  Used by the autotuner; results are
+ * identical up to float32 rounding order. */
 #define NUFFT_K2Y_COIL  0   /* (internal) lanes over coils                    */
 #define NUFFT_K2Y_ZTEAM 1   /* J lanes per point along the innermost axis     */
 #define NUFFT_K2Y_POINT 2   /* one thread per point                           */
@@ -154,6 +157,15 @@ int nufft_k2y2k(nufft_plan_t plan, const void* k, void* k_out, void* stream);
  * system ran; reading it synchronises `stream`. */
 int nufft_solve_cg(nufft_plan_t plan, const void* y, void* x, int maxiter,
                    double rtol, double atol, int* iters_out, void* stream);
+
+/* solve(y, 'L1TVOLS', maxiter, rho) (L1TVOLS, linalg/solve_cpu.py:42-163):
+ * L1 total-variation regularised least squares by split Bregman with
+ * mu = 1 and lambda = rho, maxiter outer iterations, x0 = 0; k-space
+ * preconditioner mu |xx2k(adjoint(1))| - lambda FFT(Laplacian).  Single-coil,
+ * single-instance plans.  Allocates its work vectors stream-ordered
+ * (cudaMallocAsync) and does not synchronise `stream`. */
+int nufft_solve_l1tvols(nufft_plan_t plan, const void* y, void* x, int maxiter, double rho,
+                        void* stream);
 
 /* SENSE coil operators of the deprecated reference class
  * (linalg/nufft_cpu.py:163-203).  nufft_set_sense copies coil maps of shape

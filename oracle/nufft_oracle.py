@@ -335,6 +335,50 @@ class OracleNUFFT:
             W = W / E
         return W
 
+    def l1tvols(self, y, maxiter, rho):
+        """solve(y, 'L1TVOLS', maxiter, rho): split-Bregman L1-TV least squares
+        (linalg/solve_cpu.py:42-163), mu = 1, lambda = rho, single coil, in the
+        reference's complex64 / float32 arithmetic.  The k-space preconditioner
+        is mu |xx2k(adjoint(1))| - lambda fftn(periodic Laplacian stencil)
+        (_create_kspace_sampling_density :24-40, helper.create_laplacian_kernel
+        src/_helper/helper.py:11-44); D_d x = x[n - e_d] - x[n] and its
+        transpose v[n + e_d] - v[n] (cDiff with helper.indxmap_diff :46-70)."""
+        nd = len(self.Nd)
+        lmbd = rho * 1.0
+        w = np.abs(self._xx2k1(self.adjoint(np.ones(self.M, np.complex64))))
+        lap = np.zeros(self.Kd, np.complex64)
+        lap[(0,) * nd] = -2.0 * nd
+        for d in range(nd):
+            for s in (1, -1):
+                idx = [0] * nd
+                idx[d] = s
+                lap[tuple(idx)] = 1
+        uker = w - lmbd * np.fft.fftn(lap)
+        ahy = self.adjoint(y)
+        x = np.zeros_like(ahy)
+        ahyk = np.zeros_like(ahy)
+        dd = [np.zeros(self.Nd, np.complex64) for _ in range(nd)]
+        bb = [np.zeros(self.Nd, np.complex64) for _ in range(nd)]
+        for _ in range(maxiter):
+            rhs = ahyk.copy()
+            for d in range(nd):
+                v = dd[d] - bb[d]
+                rhs += lmbd * (np.roll(v, -1, axis=d) - v)
+            x = self._k2xx1((self._xx2k1(rhs) + 1e-7) / (uker + 1e-7))
+            zz = [np.roll(x, 1, axis=d) - x for d in range(nd)]
+            st = [zz[d] + bb[d] for d in range(nd)]
+            s = np.zeros(self.Nd, np.float32)
+            for d in range(nd):
+                s = np.hypot(np.hypot(st[d].real, st[d].imag), s)
+            s = s + np.float32(1e-5)
+            th = 1.0 / lmbd
+            r = (s > th) * (s - th) / s
+            for d in range(nd):
+                dd[d] = st[d] * r
+                bb[d] += zz[d] - dd[d]
+            ahyk = ahyk - (self.selfadjoint(x) - ahy)
+        return x
+
     def solve(self, y, solver='cg', maxiter=None, rtol=1e-5, atol=0.0,
               return_info=False):
         """solve(y, 'cg', maxiter): CG on the k-space normal operator spH.sp,

@@ -52,6 +52,7 @@ SIGNATURES = {
     'nufft_k2y2k': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     'nufft_solve_cg': (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_double, c_double,
                                POINTER(c_int), c_void_p]),
+    'nufft_solve_l1tvols': (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_double, c_void_p]),
     'nufft_forward_dom': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     'nufft_set_sense': (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
     'nufft_y2k_exact_static': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -355,6 +355,17 @@ int nufft_solve_cg(nufft_plan_t p, const void* y, void* x, int maxiter, double r
                     as_stream(stream));
 }
 
+int nufft_solve_l1tvols(nufft_plan_t p, const void* y, void* x, int maxiter, double rho,
+                        void* stream) {
+    NUFFT_TRY(need_points(p, "nufft_solve_l1tvols"));
+    NUFFT_TRY(need_ptrs(y, x, "nufft_solve_l1tvols", p));
+    if (maxiter < 0) {
+        set_error("nufft_solve_l1tvols: maxiter must be non-negative");
+        return NUFFT_EINVAL;
+    }
+    return solve_l1tvols(p, (const float2*)y, (float2*)x, maxiter, rho, as_stream(stream));
+}
+
 int nufft_set_sense(nufft_plan_t p, const void* maps, int maps_on_device, void* stream) {
     NUFFT_TRY(need_plan(p, "nufft_set_sense"));
     if (p->ninst != 1) {

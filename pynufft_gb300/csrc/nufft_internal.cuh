@@ -211,4 +211,8 @@ int solve_cg(nufft_plan_s* p, const float2* y, float2* x, int maxiter, double rt
              double atol, int* iters_out, cudaStream_t s);
 void free_cg(nufft_plan_s* p);
 
+// tv.cu
+int solve_l1tvols(nufft_plan_s* p, const float2* y, float2* x, int maxiter, double rho,
+                  cudaStream_t s);
+
 }  // namespace nufft

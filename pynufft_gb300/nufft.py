@@ -417,13 +417,34 @@ class NUFFT:
                        'forward_dom')
         return self._out(out, how)
 
+    def _solve_l1tvols(self, y, maxiter=None, rho=None, **kwargs):
+        """solve(y, 'L1TVOLS', maxiter, rho) (L1TVOLS, linalg/solve_cpu.py:42-163):
+        split-Bregman L1-TV least squares, mu = 1, lambda = rho, x0 = 0."""
+        if kwargs:
+            raise TypeError('L1TVOLS() got unexpected keyword arguments ' + ', '.join(kwargs))
+        if maxiter is None or rho is None:
+            raise TypeError("L1TVOLS() needs maxiter and rho")
+        if self.batch is not None or self.ninst > 1:
+            raise NotImplementedError('L1TVOLS runs on single-coil, single-instance plans')
+        torch = _torch()
+        d, how = self._in(y, 'y')
+        out = self._empty('x')
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.nufft_solve_l1tvols(self._plan, c_void_p(d.data_ptr()),
+                                                     c_void_p(out.data_ptr()), int(maxiter),
+                                                     float(rho), self._stream()), 'solve')
+        return self._out(out, how)
+
     def solve(self, y, solver=None, *args, **kwargs):
         """solve(y, 'cg', maxiter=...) (linalg/solve_cpu.py:256-288 via
         nufft/_nufft_class_methods_cpu.py:150-166): CG on the k-space normal
         operator, x0 = 0, scipy's rtol/atol stopping rule, then k2xx(k)/sn.
-        'dc', 'lsqr' and 'lsmr' are in ``pynufft_gb300.solvers``."""
+        'L1TVOLS' runs in the library (nufft_solve_l1tvols); 'dc', 'lsqr' and
+        'lsmr' are in ``pynufft_gb300.solvers``."""
         if solver is None:
             raise ValueError('solver must be given, e.g. solve(y, "cg", maxiter=20)')
+        if solver == 'L1TVOLS':
+            return self._solve_l1tvols(y, *args, **kwargs)
         if solver != 'cg':
             from . import solvers
             return solvers.solve(self, y, solver, *args, **kwargs)

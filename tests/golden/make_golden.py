@@ -20,6 +20,11 @@ Cases (all seeds fixed):
   ndft_known_answer.npz  the exact-NDFT vectors shipped with the reference
                (tests/tmp2d_{1,2,3}_.mat: image fhat, points x, NDFT f2) and
                the reference's own J=6, K=2N forward at om = 2*pi*x.
+  l1tvols.npz  solve(y, 'L1TVOLS', maxiter, rho) of the reference on a 2D
+               radial plan (Nd 32^2) and a 3D random plan (Nd 12^3), y the
+               reference forward of a disk phantom plus 1% noise.
+
+Pass case groups (plans, radial, ndft, l1tvols) to regenerate only those.
 """
 from __future__ import annotations
 
@@ -155,12 +160,55 @@ def make_ndft_known_answer(pynufft):
     print('ndft_known_answer')
 
 
+def disk_phantom(Nd, rng):
+    """Piecewise-constant image of 6 random disks/ellipses (complex amplitudes)."""
+    grids = np.meshgrid(*[np.arange(n) - n / 2 for n in Nd], indexing='ij')
+    x = np.zeros(Nd, np.complex64)
+    for _ in range(6):
+        c = rng.uniform(-0.3, 0.3, len(Nd)) * np.array(Nd)
+        a = rng.uniform(0.08, 0.3, len(Nd)) * np.array(Nd)
+        inside = sum(((g - ci) / ai) ** 2 for g, ci, ai in zip(grids, c, a)) <= 1
+        x[inside] += complex(rng.standard_normal(), rng.standard_normal())
+    return x
+
+
+def make_l1tvols(pynufft):
+    """solve(y, 'L1TVOLS', maxiter, rho) on 2D radial and 3D random plans."""
+    out = {}
+    rng = np.random.default_rng(11)
+    ang = np.arange(48) * np.pi / 48
+    rad = np.linspace(-np.pi, np.pi, 64, endpoint=False)
+    om2 = np.stack([(np.cos(ang)[:, None] * rad).ravel(), (np.sin(ang)[:, None] * rad).ravel()], 1)
+    om3 = rng.uniform(-np.pi, np.pi, (6000, 3))
+    for tag, om, Nd, Kd, Jd, it, rho in (('2d', om2, (32, 32), (64, 64), (6, 6), 6, 0.1),
+                                         ('3d', om3, (12, 12, 12), (24, 24, 24), (6, 6, 6), 4, 0.5)):
+        A = pynufft.NUFFT()
+        A.plan(om, Nd, Kd, Jd)
+        x = disk_phantom(Nd, rng)
+        y = A.forward(x).astype(np.complex64)
+        y = (y + 0.01 * np.abs(y).mean() * cplx(rng, y.shape)).astype(np.complex64)
+        out[f'om_{tag}'] = om
+        out[f'geom_{tag}'] = np.array([Nd, Kd, Jd])
+        out[f'y_{tag}'] = y
+        out[f'maxiter_{tag}'] = it
+        out[f'rho_{tag}'] = rho
+        out[f'x_{tag}'] = A.solve(y, 'L1TVOLS', maxiter=it, rho=rho)
+    np.savez_compressed(os.path.join(HERE, 'l1tvols.npz'), **out)
+    print('l1tvols')
+
+
 def main():
     pynufft, helper = _import_reference()
-    for name, args in PLAN_CASES.items():
-        make_plan_case(pynufft, helper, name, *args)
-    make_radial_c1(pynufft)
-    make_ndft_known_answer(pynufft)
+    only = sys.argv[1:]
+    if not only or 'plans' in only:
+        for name, args in PLAN_CASES.items():
+            make_plan_case(pynufft, helper, name, *args)
+    if not only or 'radial' in only:
+        make_radial_c1(pynufft)
+    if not only or 'ndft' in only:
+        make_ndft_known_answer(pynufft)
+    if not only or 'l1tvols' in only:
+        make_l1tvols(pynufft)
 
 
 if __name__ == '__main__':

@@ -71,3 +71,40 @@ def test_least_squares_solvers_match_scipy_on_the_oracle(solver):
     assert rel_l2(x, ref) < 1e-3, rel_l2(x, ref)
     x2 = A.solve(y, solver, iter_lim=8, atol=0.0, btol=0.0)
     assert rel_l2(x2, x) < 1e-6
+
+
+@pytest.mark.parametrize('tag', ['2d', '3d'])
+def test_l1tvols_matches_reference(tag):
+    """solve(y, 'L1TVOLS', maxiter, rho) through nufft_solve_l1tvols against
+    the reference's own result (tests/golden/l1tvols.npz) and the oracle.
+    The shrinkage makes the iteration nonlinear, so float32 rounding grows a
+    little over the iterations: 1e-4 relative L2."""
+    from conftest import load_golden
+    from pynufft_gb300 import NUFFT
+    g = load_golden('l1tvols')
+    Nd, Kd, Jd = [tuple(int(v) for v in r) for r in g[f'geom_{tag}']]
+    it, rho = int(g[f'maxiter_{tag}']), float(g[f'rho_{tag}'])
+    A = NUFFT(0)
+    A.plan(g[f'om_{tag}'], Nd, Kd, Jd)
+    x = A.solve(g[f'y_{tag}'], 'L1TVOLS', maxiter=it, rho=rho)
+    assert x.shape == Nd and x.dtype == np.complex64
+    assert rel_l2(x, g[f'x_{tag}']) < 1e-4
+    x0 = A.solve(g[f'y_{tag}'], 'L1TVOLS', maxiter=0, rho=rho)
+    assert not np.any(x0)
+
+
+def test_l1tvols_rejects_bad_arguments():
+    from pynufft_gb300 import NUFFT
+    rng = np.random.default_rng(3)
+    om = rng.uniform(-np.pi, np.pi, (500, 2))
+    A = NUFFT(0)
+    A.plan(om, (16, 16), (32, 32), (6, 6))
+    y = cplx(rng, (500,))
+    with pytest.raises(ValueError):
+        A.solve(y, 'L1TVOLS', maxiter=2, rho=0.0)
+    with pytest.raises(TypeError):
+        A.solve(y, 'L1TVOLS', maxiter=2)
+    B = NUFFT(0)
+    B.plan(om, (16, 16), (32, 32), (6, 6), batch=2)
+    with pytest.raises(NotImplementedError):
+        B.solve(cplx(rng, (500, 2)), 'L1TVOLS', maxiter=2, rho=0.1)

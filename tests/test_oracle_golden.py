@@ -120,3 +120,15 @@ def test_oracle_adjoint_identity():
     lhs = np.vdot(O.forward(x), y)
     rhs = np.prod((40, 48)) * np.vdot(x, O.adjoint(y))
     assert abs(lhs - rhs) / abs(lhs) < 1e-5
+
+
+@pytest.mark.parametrize('tag', ['2d', '3d'])
+def test_oracle_l1tvols_matches_reference(tag):
+    """The oracle's split-Bregman L1-TV restatement reproduces the
+    reference's solve(y, 'L1TVOLS', maxiter, rho) (linalg/solve_cpu.py:42-163)."""
+    g = load_golden('l1tvols')
+    Nd, Kd, Jd = [tuple(int(v) for v in r) for r in g[f'geom_{tag}']]
+    O = OracleNUFFT()
+    O.plan(g[f'om_{tag}'], Nd, Kd, Jd)
+    x = O.l1tvols(g[f'y_{tag}'], int(g[f'maxiter_{tag}']), float(g[f'rho_{tag}']))
+    assert rel_l2(x, g[f'x_{tag}']) < 1e-6
