@@ -42,6 +42,7 @@ extern "C" {
 #define NUFFT_ENOPOINTS          6  /* nufft_set_points has not been called   */
 #define NUFFT_ECG_BREAKDOWN      7  /* CG: p^H A p <= 0 or not finite         */
 #define NUFFT_EUNSUPPORTED       8  /* valid request this build does not do   */
+#define NUFFT_ETIMEOUT           9  /* a kernel's bounded wait ran out        */
 
 /* ---- plan flags */
 #define NUFFT_FLAG_DETERMINISTIC 1  /* bitwise-reproducible gridding (y2k)    */
@@ -115,6 +116,12 @@ int nufft_plan_set_bins(nufft_plan_t plan, const int* bin_shape, int max_sub_poi
 #define NUFFT_Y2K_GLOBAL 3  /* z-teams adding floats straight into the grid
                                (no shared tile; not in deterministic mode)    */
 int nufft_plan_set_methods(nufft_plan_t plan, int k2y_method, int y2k_method);
+
+/* Synchronise `stream` and report whether any kernel of this plan gave up a
+ * bounded wait for its asynchronous (bulk-copy) loads since the last check:
+ * NUFFT_ETIMEOUT if so (that launch's output is incomplete; the flag is
+ * cleared), else NUFFT_OK.  No counterpart in the reference. */
+int nufft_plan_check(nufft_plan_t plan, void* stream);
 
 /* Query plan geometry: total points, number of gridding sub-problems and
  * bytes of device memory the plan holds. */

@@ -22,6 +22,7 @@ NUFFT_ECUFFT = 5
 NUFFT_ENOPOINTS = 6
 NUFFT_ECG_BREAKDOWN = 7
 NUFFT_EUNSUPPORTED = 8
+NUFFT_ETIMEOUT = 9
 NUFFT_FLAG_DETERMINISTIC = 1
 NUFFT_K2Y_ZTEAM, NUFFT_K2Y_POINT, NUFFT_K2Y_TILE, NUFFT_K2Y_TILE_POINT = 1, 2, 3, 4
 NUFFT_Y2K_ZTEAM, NUFFT_Y2K_POINT, NUFFT_Y2K_GLOBAL = 1, 2, 3
@@ -53,6 +54,7 @@ SIGNATURES = {
     'nufft_solve_cg': (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_double, c_double,
                                POINTER(c_int), c_void_p]),
     'nufft_solve_l1tvols': (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_double, c_void_p]),
+    'nufft_plan_check': (c_int, [c_void_p, c_void_p]),
     'nufft_forward_dom': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     'nufft_set_sense': (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
     'nufft_y2k_exact_static': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -45,6 +45,7 @@ nufft::Geom nufft_plan_s::geom() const {
         if (d < ndim && c) c += (size_t)Ma * g.JP[d];
     }
     g.wpt = d_wpt;
+    g.kerr = d_kerr;
     g.sub = d_sub;
     g.nsub = nsub;
     // lane mappings: coil-teams for B >= 8; otherwise the plan's choice.  The
@@ -165,6 +166,8 @@ int nufft_plan_create(int ndim, const int* Nd, const int* Kd, const int* Jd, int
     if (e == cudaSuccess) e = cudaMalloc(&p->d_axc, sizeof(AxisConst) * 3);
     const size_t ncell = (size_t)ninst * p->prodK * batch;
     if (e == cudaSuccess) e = cudaMalloc(&p->d_grid, sizeof(float2) * ncell);
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_kerr, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p->d_kerr, 0, sizeof(int));
     if (e != cudaSuccess) {
         set_error(std::string("nufft_plan_create: ") + cudaGetErrorString(e));
         return fail(e == cudaErrorMemoryAllocation ? NUFFT_ENOMEM : NUFFT_ECUDA);
@@ -187,6 +190,7 @@ int nufft_plan_destroy(nufft_plan_t p) {
     cudaFree(p->d_igrid);
     cudaFree(p->d_dscal);
     cudaFree(p->d_maps);
+    cudaFree(p->d_kerr);
     delete p;
     return NUFFT_OK;
 }
@@ -264,6 +268,21 @@ int nufft_plan_info(nufft_plan_t p, int64_t* M_total, int64_t* n_sub, int64_t* d
             pts += (int64_t)p->ybuf_elems * 8 + p->nsub * 16;
         }
         *device_bytes = (int64_t)p->dev_bytes + pts;
+    }
+    return NUFFT_OK;
+}
+
+int nufft_plan_check(nufft_plan_t p, void* stream) {
+    NUFFT_TRY(need_plan(p, "nufft_plan_check"));
+    int h = 0;
+    cudaStream_t s = as_stream(stream);
+    NUFFT_CUDA_TRY(cudaMemcpyAsync(&h, p->d_kerr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h != 0) {
+        NUFFT_CUDA_TRY(cudaMemsetAsync(p->d_kerr, 0, sizeof(int), s));
+        set_error("a kernel's wait for its asynchronous copies ran out (code " + std::to_string(h) +
+                  "); its output is incomplete");
+        return NUFFT_ETIMEOUT;
     }
     return NUFFT_OK;
 }

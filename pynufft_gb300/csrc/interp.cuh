@@ -490,6 +490,44 @@ __global__ void __launch_bounds__(256) k2y_tile_kernel(Geom g, const float2* __r
 // banks from its first, so a warp's 32 accesses of one tap fall in 32
 // distinct banks whenever the bin's keys allow it.
 // ---------------------------------------------------------------------------
+// ---- bulk-copy engine (cp.async.bulk) and mbarrier helpers -----------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+// global -> shared copy of `bytes` (multiple of 16, both addresses 16-byte
+// aligned) that completes `bytes` transactions on `bar`
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+// Wait for phase `parity` of `bar` with a bounded number of polls (each poll
+// may suspend the thread for a hardware-chosen interval); false if it ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (int i = 0; i < (1 << 22); ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
 template <int DIM>
 __device__ __forceinline__ int tile_addr(const int (&t)[3], const TileStrides& ts) {
     if constexpr (DIM == 3) return t[0] * ts.sx + t[1] * ts.sy + t[2];
@@ -497,8 +535,13 @@ __device__ __forceinline__ int tile_addr(const int (&t)[3], const TileStrides& t
     else return t[0];
 }
 
-// k2y from the shared tile.  EX: every axis has exactly JM taps.
-template <int DIM, int JM, bool EX>
+// k2y from the shared tile.  EX: every axis has exactly JM taps.  BULK (one
+// coil, 2D/3D, even K and bin along z, tile row no longer than the grid row):
+// the tile rows arrive by bulk copies (one or two per row, the second where
+// the row wraps around the periodic grid) completing on one mbarrier; the
+// bounded wait sets the plan's error flag and returns if the copies never
+// land.  Otherwise every thread loads cells through registers.
+template <int DIM, int JM, bool EX, bool BULK>
 __global__ void __launch_bounds__(128) k2y_spoint_kernel(Geom g, const float2* __restrict__ grid,
                                                          float2* __restrict__ y) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -526,11 +569,45 @@ __global__ void __launch_bounds__(128) k2y_spoint_kernel(Geom g, const float2* _
     const int end = sp.y + sp.z;
 
     for (int b = 0; b < B; ++b) {
-        TileWalk<DIM> w;
-        w.init(g.T, threadIdx.x, blockDim.x);
-        for (int c = threadIdx.x; c < ncell; c += blockDim.x, w.next())
-            tile[tile_addr<DIM>(w.t, ts)] = __ldg(grid + (ibase + w.cell(g, o)) * B + b);
-        __syncthreads();
+        if constexpr (BULK) {
+            __shared__ __align__(8) uint64_t s_bar;
+            const int rowlen = (g.T[DI] + 1) & ~1;   // cells per row, even
+            const int nrows = (DIM == 3) ? g.T[0] * g.T[1] : g.T[0];
+            if (threadIdx.x == 0) {
+                mbar_init(&s_bar, 1);
+                mbar_arrive_expect_tx(&s_bar, (uint32_t)(nrows * rowlen) * 8u);
+            }
+            __syncthreads();
+            const int Kz = g.K[DI], oz = o[DI];
+            const int n1 = min(rowlen, Kz - oz);
+            for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+                size_t rowcell;
+                float2* dst;
+                if constexpr (DIM == 3) {
+                    const int rx = r / g.T[1], ry = r - rx * g.T[1];
+                    rowcell = ((size_t)wrapn(o[0] + rx, g.K[0]) * g.K[1] + wrapn(o[1] + ry, g.K[1])) * Kz;
+                    dst = tile + rx * ts.sx + ry * ts.sy;
+                } else {
+                    rowcell = (size_t)wrapn(o[0] + r, g.K[0]) * Kz;
+                    dst = tile + r * ts.sy;
+                }
+                const float2* src = grid + ibase + rowcell;
+                bulk_g2s(dst, src + oz, (uint32_t)n1 * 8u, &s_bar);
+                if (n1 < rowlen) bulk_g2s(dst + n1, src, (uint32_t)(rowlen - n1) * 8u, &s_bar);
+            }
+            const bool ok = mbar_wait_bounded(&s_bar, 0);
+            if (__syncthreads_or(!ok)) {
+                if (threadIdx.x == 0) atomicExch(g.kerr, 1);
+                mbar_wait_bounded(&s_bar, 0);   // a second bound for copies still in flight
+                return;
+            }
+        } else {
+            TileWalk<DIM> w;
+            w.init(g.T, threadIdx.x, blockDim.x);
+            for (int c = threadIdx.x; c < ncell; c += blockDim.x, w.next())
+                tile[tile_addr<DIM>(w.t, ts)] = __ldg(grid + (ibase + w.cell(g, o)) * B + b);
+            __syncthreads();
+        }
         for (int base_s = sp.y; base_s < end; base_s += per_round) {
             const int s = base_s + (int)(threadIdx.x >> 5) * PW + pw;
             const bool active = s < end;

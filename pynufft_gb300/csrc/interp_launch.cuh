@@ -34,7 +34,15 @@ static void k2y_launch(const Geom& g, const float2* grid, float2* y, cudaStream_
             if (paired) {
                 bool exact = true;
                 for (int d = 0; d < DIM; ++d) exact = exact && (g.J[d] == JM);
-                kern = exact ? k2y_spoint_kernel<DIM, JM, true> : k2y_spoint_kernel<DIM, JM, false>;
+                const int Kz = g.K[DIM - 1], rowlen = (g.T[DIM - 1] + 1) & ~1;
+                const bool bulk = DIM > 1 && g.B == 1 && Kz % 2 == 0 && g.bs[DIM - 1] % 2 == 0 &&
+                                  rowlen <= Kz && (reinterpret_cast<uintptr_t>(grid) & 15) == 0;
+                if (bulk)
+                    kern = exact ? k2y_spoint_kernel<DIM, JM, true, true>
+                                 : k2y_spoint_kernel<DIM, JM, false, true>;
+                else
+                    kern = exact ? k2y_spoint_kernel<DIM, JM, true, false>
+                                 : k2y_spoint_kernel<DIM, JM, false, false>;
                 nt = 128;
             }
             if (smem > 48 * 1024)

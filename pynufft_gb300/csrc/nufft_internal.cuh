@@ -59,13 +59,16 @@ struct Geom {
     int64_t nsub;
     int kmethod;                 // k2y lane mapping (NUFFT_K2Y_*), resolved
     int ymethod;                 // y2k lane mapping (NUFFT_Y2K_*), resolved
+    int* kerr;                   // device flag: a bounded wait ran out (nufft_plan_check)
 };
 
 // Padded shared-tile layout of the paired-thread kernels: tile cell
 // (x, y, z) (z fastest; tile extents T) sits at word x*sx + y*sy + z.  The
 // stride of the axis whose taps the two threads of a point split (x in 3D,
 // y in 2D) is padded to 16 mod 32, so the two threads of a point always
-// address words 16 banks apart; n is the padded cell count.
+// address words 16 banks apart; rows (sy) are even, so a row of complex64
+// cells starts on a 16-byte boundary (bulk-copy destinations); n is the
+// padded cell count.
 struct TileStrides {
     int sy, sx, n;
 };
@@ -76,8 +79,8 @@ __host__ __device__ inline TileStrides tile_strides(int ndim, const int* T) {
         s.sy = pad_to_16_mod_32(T[1]);
         s.n = T[0] * s.sy;
     } else if (ndim == 3) {
-        s.sy = T[2];
-        s.sx = pad_to_16_mod_32(T[1] * T[2]);
+        s.sy = (T[2] + 1) & ~1;
+        s.sx = pad_to_16_mod_32(T[1] * s.sy);
         s.n = T[0] * s.sx;
     }
     return s;
@@ -108,6 +111,7 @@ struct nufft_plan_s {
     float2* d_grid = nullptr;         // ninst * prodK * B oversampled grid workspace
     float2* d_ybuf = nullptr;         // M * B sample workspace (selfadjoint, CG)
     float2* d_maps = nullptr;         // coil sensitivities Nd x B (nufft_set_sense)
+    int* d_kerr = nullptr;            // device error flag written by bounded waits
     size_t ybuf_elems = 0;
 
     // point data (valid after nufft_set_points)

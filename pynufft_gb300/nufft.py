@@ -232,6 +232,12 @@ class NUFFT:
         _lib.check(self._lib.nufft_plan_set_methods(self._plan, km, ym), 'set_methods')
         self.methods = (k2y, y2k)
 
+    def check(self):
+        """Synchronise the plan's stream and raise NufftError if a kernel gave up
+        a bounded wait for its asynchronous loads since the last check
+        (nufft_plan_check)."""
+        _lib.check(self._lib.nufft_plan_check(self._plan, self._stream()), 'check')
+
     def info(self):
         m, ns, by = c_int64(), c_int64(), c_int64()
         _lib.check(self._lib.nufft_plan_info(self._plan, ctypes.byref(m), ctypes.byref(ns),

@@ -289,6 +289,7 @@ def test_every_lane_mapping_matches_reference(NUFFT, case, k2y, y2k):
     assert rel_l2(A.y2k(g['y']), g['y2k']) < TOL
     assert rel_l2(A.forward(g['x']), g['forward']) < TOL
     assert rel_l2(A.adjoint(g['y']), g['adjoint']) < TOL
+    A.check()   # no kernel gave up a bounded wait for its bulk copies
 
 
 @pytest.mark.parametrize('bins', [(4, 4), (16, 8), (64, 64)])
