@@ -77,15 +77,30 @@ __device__ void block_dot(const CGGeom& g, const float2* __restrict__ a,
     if (q == 0) part[((size_t)inst * g.nblk + blockIdx.x) * g.B + b] = red[t];
 }
 
-__device__ __forceinline__ double2 sum_parts(const CGGeom& g, const double2* part, int s) {
+// Sum of one system's per-block partials by a whole block (launched with one
+// block of kSumThreads threads per system): strided partial sums, then a
+// fixed-order tree, so the result does not depend on timing.  Every thread
+// of the block receives the total.
+constexpr int kSumThreads = 256;
+__device__ double2 sum_parts(const CGGeom& g, const double2* part, int s) {
+    __shared__ double2 red[kSumThreads];
     const int inst = s / g.B, b = s % g.B;
     double re = 0.0, im = 0.0;
-    for (int k = 0; k < g.nblk; ++k) {
+    for (int k = threadIdx.x; k < g.nblk; k += blockDim.x) {
         const double2 v = part[((size_t)inst * g.nblk + k) * g.B + b];
         re += v.x;
         im += v.y;
     }
-    return make_double2(re, im);
+    red[threadIdx.x] = make_double2(re, im);
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            red[threadIdx.x].x += red[threadIdx.x + o].x;
+            red[threadIdx.x].y += red[threadIdx.x + o].y;
+        }
+        __syncthreads();
+    }
+    return red[0];
 }
 
 // r = b (already in r), x = 0; rho = ||b||^2; tol = max(atol, rtol ||b||)
@@ -95,9 +110,9 @@ __global__ void cg_norm_kernel(CGGeom g, const float2* __restrict__ r, double2* 
 
 __global__ void cg_init_sys_kernel(CGGeom g, const double2* __restrict__ part,
                                    CGSys* __restrict__ sys, double rtol, double atol, int maxiter) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= g.S) return;
+    const int s = blockIdx.x;   // one block per system
     const double rho = sum_parts(g, part, s).x;
+    if (threadIdx.x != 0) return;
     const double bn = sqrt(rho);
     CGSys st{};
     st.rho = rho;
@@ -108,21 +123,24 @@ __global__ void cg_init_sys_kernel(CGGeom g, const double2* __restrict__ part,
     sys[s] = st;
 }
 
-// p = r (first iteration) or p = r + beta p
+// p = r (first iteration) or p = r + beta p; grid (nblk, ninst), thread t
+// serves coil t % B like the reductions
 __global__ void cg_update_p_kernel(CGGeom g, const CGSys* __restrict__ sys,
                                    const float2* __restrict__ r, float2* __restrict__ p) {
-    const int64_t n = (int64_t)g.ninst * g.prodK * g.B;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int b = (int)(e % g.B);
-        const int inst = (int)(e / ((int64_t)g.prodK * g.B));
-        const CGSys& st = sys[inst * g.B + b];
-        if (st.done) continue;
+    const int inst = blockIdx.y;
+    const int t = threadIdx.x, b = t % g.B, q = t / g.B;
+    const CGSys& st = sys[inst * g.B + b];
+    if (st.done) return;
+    const bool first = st.iters == 0;
+    const float beta = first ? 0.f : (float)(st.rho / st.rho_prev);
+    const int64_t chunk = (g.prodK + g.nblk - 1) / g.nblk;
+    const int64_t c0 = blockIdx.x * chunk, c1 = min(g.prodK, c0 + chunk);
+    for (int64_t c = c0 + q; c < c1; c += g.Q) {
+        const size_t e = ((size_t)inst * g.prodK + c) * g.B + b;
         const float2 rv = r[e];
-        if (st.iters == 0) {
+        if (first) {
             p[e] = rv;
         } else {
-            const float beta = (float)(st.rho / st.rho_prev);
             const float2 pv = p[e];
             p[e] = make_float2(fmaf(beta, pv.x, rv.x), fmaf(beta, pv.y, rv.y));
         }
@@ -135,11 +153,11 @@ __global__ void cg_dot_kernel(CGGeom g, const float2* __restrict__ p, const floa
 }
 
 __global__ void cg_alpha_kernel(CGGeom g, const double2* __restrict__ part, CGSys* __restrict__ sys) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= g.S) return;
-    CGSys st = sys[s];
-    if (st.done) return;
+    const int s = blockIdx.x;   // one block per system
+    if (sys[s].done) return;
     const double2 pq = sum_parts(g, part, s);
+    if (threadIdx.x != 0) return;
+    CGSys st = sys[s];
     st.pq_re = pq.x;
     st.pq_im = pq.y;
     const double den = pq.x * pq.x + pq.y * pq.y;
@@ -202,12 +220,13 @@ __global__ void cg_axpy_kernel(CGGeom g, const CGSys* __restrict__ sys, const fl
 }
 
 __global__ void cg_finalize_kernel(CGGeom g, const double2* __restrict__ part, CGSys* __restrict__ sys) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= g.S) return;
+    const int s = blockIdx.x;   // one block per system
+    if (sys[s].done) return;
+    const double rho = sum_parts(g, part, s).x;
+    if (threadIdx.x != 0) return;
     CGSys st = sys[s];
-    if (st.done) return;
     st.rho_prev = st.rho;
-    st.rho = sum_parts(g, part, s).x;
+    st.rho = rho;
     st.iters += 1;
     if (sqrt(st.rho) < st.tol || st.iters >= st.maxiter) st.done = 1;
     sys[s] = st;
@@ -236,7 +255,9 @@ static CGGeom cg_geom(const nufft_plan_s* p) {
     int Q = 1;
     while (Q * 2 * p->B <= 256) Q *= 2;
     g.Q = Q;
-    int64_t want = std::max<int64_t>(1, (int64_t)p->num_sms * 2 / std::max(1, p->ninst));
+    // enough blocks for 8 per SM in total (latency hiding for the streaming
+    // vector kernels); their partials are summed by a whole block per system
+    int64_t want = std::max<int64_t>(1, (int64_t)p->num_sms * 8 / std::max(1, p->ninst));
     g.nblk = (int)std::min<int64_t>(want, std::max<int64_t>(1, p->prodK / (8 * Q)));
     return g;
 }
@@ -250,12 +271,11 @@ static int issue_init(nufft_plan_s* p, const CGGeom& g, const float2* y, int max
     CGSys* sys = reinterpret_cast<CGSys*>(p->d_cgs);
     double2* part = reinterpret_cast<double2*>(p->d_part);
     const dim3 rgrid(g.nblk, g.ninst);
-    const int sthreads = 128, sblocks = (g.S + sthreads - 1) / sthreads;
     NUFFT_CUDA_TRY(cudaMemsetAsync(xk, 0, sizeof(float2) * n, s));
     NUFFT_TRY(launch_y2k(p, y, r, s));
     cg_norm_kernel<<<rgrid, g.B * g.Q, 0, s>>>(g, r, part);
     NUFFT_TRY(check_launch("cg_norm_kernel"));
-    cg_init_sys_kernel<<<sblocks, sthreads, 0, s>>>(g, part, sys, rtol, atol, maxiter);
+    cg_init_sys_kernel<<<g.S, kSumThreads, 0, s>>>(g, part, sys, rtol, atol, maxiter);
     return check_launch("cg_init_sys_kernel");
 }
 
@@ -270,20 +290,18 @@ static int issue_iters(nufft_plan_s* p, const CGGeom& g, int iters, cudaStream_t
     double2* part = reinterpret_cast<double2*>(p->d_part);
     const dim3 rgrid(g.nblk, g.ninst);
     const int rthreads = g.B * g.Q;
-    const int sthreads = 128, sblocks = (g.S + sthreads - 1) / sthreads;
-    const int eblocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)p->num_sms * 16));
     for (int it = 0; it < iters; ++it) {
-        cg_update_p_kernel<<<eblocks, 256, 0, s>>>(g, sys, r, pv);
+        cg_update_p_kernel<<<rgrid, rthreads, 0, s>>>(g, sys, r, pv);
         NUFFT_TRY(check_launch("cg_update_p_kernel"));
         NUFFT_TRY(launch_k2y(p, pv, p->d_ybuf, s));          // q = spH sp p
         NUFFT_TRY(launch_y2k(p, p->d_ybuf, q, s));
         cg_dot_kernel<<<rgrid, rthreads, 0, s>>>(g, pv, q, part);
         NUFFT_TRY(check_launch("cg_dot_kernel"));
-        cg_alpha_kernel<<<sblocks, sthreads, 0, s>>>(g, part, sys);
+        cg_alpha_kernel<<<g.S, kSumThreads, 0, s>>>(g, part, sys);
         NUFFT_TRY(check_launch("cg_alpha_kernel"));
         cg_axpy_kernel<<<rgrid, rthreads, 0, s>>>(g, sys, pv, q, xk, r, part);
         NUFFT_TRY(check_launch("cg_axpy_kernel"));
-        cg_finalize_kernel<<<sblocks, sthreads, 0, s>>>(g, part, sys);
+        cg_finalize_kernel<<<g.S, kSumThreads, 0, s>>>(g, part, sys);
         NUFFT_TRY(check_launch("cg_finalize_kernel"));
     }
     return NUFFT_OK;
