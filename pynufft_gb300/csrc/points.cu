@@ -129,6 +129,18 @@ __global__ void scan_kernel(const int* __restrict__ in, int* __restrict__ out, i
     if (tid == blockDim.x - 1) out[n] = (int)part[tid];
 }
 
+// 1/x in FP64 (x normal, |x| well inside the float range) from a float32
+// reciprocal refined by two Newton-Raphson steps y <- y + y (1 - x y): the
+// relative error squares at each step (~2^-23 -> ~2^-46 -> below FP64
+// rounding), at four FMAs instead of a full FP64 division.
+__device__ __forceinline__ double rcp_newton(double x) {
+    double y = (double)__frcp_rn((float)x);
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
 __device__ __forceinline__ double sinc_direct(double x) {
     if (x == 0.0) return 1.0;
     return sinpi(x) / (M_PI * x);
@@ -146,7 +158,8 @@ __device__ __forceinline__ double sinc_direct(double x) {
 // |dk + n| < 1 are evaluated directly so the sinc keeps full relative
 // accuracy near its peak.  The J phase factors come from one sincos rotated
 // by the tabulated exp(-i gam (N-1)/2 j).  This GPU's FP64 rate is low, so
-// divisions and transcendental calls are kept to a few per axis.
+// transcendental calls are kept to a few per axis and the sinc denominators
+// use a Newton-refined reciprocal instead of FP64 divisions.
 __device__ float axis_coefs(const AxisConst& a, const AxisTab& tab, double w,
                             float2* __restrict__ out) {
     const int J = a.J, L = a.L;
@@ -162,7 +175,7 @@ __device__ float axis_coefs(const AxisConst& a, const AxisTab& tab, double w,
         const double xn = dk + n;
         const int q = n + L + J;
         sv[q] = (fabs(xn) < 1.0) ? sinc_direct(xn * a.inv_ratio)
-                                 : (s0 * tab.cs[q] + c0 * tab.ss[q]) / (pr * xn);
+                                 : (s0 * tab.cs[q] + c0 * tab.ss[q]) * rcp_newton(pr * xn);
     }
     double r[NUFFT_MAXJ];
     for (int j = 1; j <= J; ++j) {
@@ -299,6 +312,8 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     }
     if (M >= (int64_t)1 << 31) { set_error("nufft_set_points: more than 2^31-1 points"); return NUFFT_EINVAL; }
     if (M > 0 && !om) { set_error("nufft_set_points: om is NULL"); return NUFFT_EINVAL; }
+    // captured CG graphs hold the old tables' pointers: drop them with the tables
+    free_cg(p);
     free_points(p);
     p->counts.assign(counts, counts + p->ninst);
     default_bins(p, p->bs, p->maxsub);

@@ -127,24 +127,35 @@ class NUFFT:
 
     def _plan_common(self, oms, Nd, Kd, Jd, batch, B, ninst, deterministic, bins, max_sub):
         torch = _torch()
-        self.release()
         ndim = len(Nd)
         flags = _lib.NUFFT_FLAG_DETERMINISTIC if deterministic else 0
-        h = c_void_p()
+        key = (tuple(Nd), tuple(Kd), tuple(Jd), B, ninst, flags,
+               None if bins is None else tuple(bins), max_sub)
+        reuse = (self._plan is not None and getattr(self, '_key', None) == key
+                 and getattr(self, '_maps', None) is None)
         with torch.cuda.device(self.device):
-            _lib.check(self._lib.nufft_plan_create(ndim, _lib.int_array(Nd), _lib.int_array(Kd),
-                                                   _lib.int_array(Jd), B, ninst, flags,
-                                                   ctypes.byref(h)), 'plan')
-            self._plan = h
-            self._alpha = []
-            for d in range(ndim):
-                a, L = alpha_fit(int(Nd[d]), int(Jd[d]), int(Kd[d]))
-                self._alpha.append((a, L))
-                buf = (ctypes.c_float * 16)(*([float(v) for v in a] + [0.0] * (16 - a.size)))
-                _lib.check(self._lib.nufft_plan_set_alpha(h, d, buf, int(L)), 'plan')
-            if bins is not None or max_sub is not None:
-                bs = _lib.int_array(bins) if bins is not None else None
-                _lib.check(self._lib.nufft_plan_set_bins(h, bs, int(max_sub or 0)), 'plan')
+            if reuse:
+                # same geometry: keep the plan (FFT plans, scaling factors and
+                # interpolator coefficients); only the points are replaced
+                h = self._plan
+            else:
+                self.release()
+                h = c_void_p()
+                _lib.check(self._lib.nufft_plan_create(ndim, _lib.int_array(Nd), _lib.int_array(Kd),
+                                                       _lib.int_array(Jd), B, ninst, flags,
+                                                       ctypes.byref(h)), 'plan')
+                self._plan = h
+                self._alpha = []
+                for d in range(ndim):
+                    a, L = alpha_fit(int(Nd[d]), int(Jd[d]), int(Kd[d]))
+                    self._alpha.append((a, L))
+                    buf = (ctypes.c_float * 16)(*([float(v) for v in a] + [0.0] * (16 - a.size)))
+                    _lib.check(self._lib.nufft_plan_set_alpha(h, d, buf, int(L)), 'plan')
+                if bins is not None or max_sub is not None:
+                    bs = _lib.int_array(bins) if bins is not None else None
+                    _lib.check(self._lib.nufft_plan_set_bins(h, bs, int(max_sub or 0)), 'plan')
+                self._key = None
+                self._sn_cache = None
             counts = []
             parts = []
             on_dev = False
@@ -162,6 +173,7 @@ class NUFFT:
             cnt = (c_int64 * ninst)(*counts)
             _lib.check(self._lib.nufft_set_points(h, cnt, c_void_p(ptr), 1 if on_dev else 0,
                                                   self._stream()), 'plan')
+            self._key = key
         self.Nd, self.Kd, self.Jd = tuple(Nd), tuple(Kd), tuple(Jd)
         self.ndims = ndim
         self.ft_axes = tuple(range(ndim))
@@ -174,7 +186,9 @@ class NUFFT:
         self.Kdprod = int(numpy.prod(Kd))
         self.Jdprod = int(numpy.prod(Jd))
         self.st = {'M': numpy.int32(sum(counts)), 'Nd': self.Nd, 'Kd': self.Kd, 'Jd': self.Jd}
-        self.sn = self._host_sn()
+        if getattr(self, '_sn_cache', None) is None:
+            self._sn_cache = self._host_sn()
+        self.sn = self._sn_cache
         return 0
 
     def _om_tensor(self, om, ndim):
@@ -213,6 +227,8 @@ class NUFFT:
         if getattr(self, '_plan', None) is not None:
             self._lib.nufft_plan_destroy(self._plan)
             self._plan = None
+        self._key = None
+        self._maps = None
 
     def __del__(self):
         try:

@@ -315,3 +315,25 @@ def test_autotune_picks_a_setting_and_keeps_results(NUFFT, tmp_path, monkeypatch
     B = NUFFT(0)
     B.plan(g['om'], (12, 12, 12), (24, 24, 24), (6, 6, 6), autotune=True)   # from the cache
     assert B.tuned == A.tuned
+
+
+def test_replan_same_geometry_matches_fresh_plan(NUFFT):
+    """plan() again with the same geometry keeps the plan and replaces only
+    the points (and drops the captured CG graphs, which hold the old
+    tables): results equal a fresh plan's."""
+    rng = np.random.default_rng(21)
+    Nd, Kd, Jd = (24, 20), (48, 40), (6, 6)
+    om1 = rng.uniform(-np.pi, np.pi, (1500, 2))
+    om2 = rng.uniform(-np.pi, np.pi, (2300, 2))
+    x = cplx(rng, Nd)
+    A = NUFFT(0)
+    A.plan(om1, Nd, Kd, Jd)
+    y1 = cplx(rng, (1500,))
+    A.solve(y1, 'cg', maxiter=3)
+    A.plan(om2, Nd, Kd, Jd)
+    B = NUFFT(0)
+    B.plan(om2, Nd, Kd, Jd)
+    assert np.array_equal(A.forward(x), B.forward(x))
+    y2 = cplx(rng, (2300,))
+    assert rel_l2(A.adjoint(y2), B.adjoint(y2)) < 1e-6
+    assert rel_l2(A.solve(y2, 'cg', maxiter=3), B.solve(y2, 'cg', maxiter=3)) < 1e-5
