@@ -160,49 +160,116 @@ __device__ __forceinline__ double sinc_direct(double x) {
 // by the tabulated exp(-i gam (N-1)/2 j).  This GPU's FP64 rate is low, so
 // transcendental calls are kept to a few per axis and the sinc denominators
 // use a Newton-refined reciprocal instead of FP64 divisions.
-__device__ float axis_coefs(const AxisConst& a, const AxisTab& tab, double w,
-                            float2* __restrict__ out) {
+// FP64 min-max coefficients c_j(dk), j = 0..J-1, of one axis:
+//   r_j = sum_l alpha_|l| sinc((dk - j + l) N/K)   (nufft_r), c = T r (min_max).
+// Each sinc value (index n = l - j in [-(L+J), L-1]) is added straight into
+// the register accumulators of the J outputs it feeds (l ascending for every
+// j, as a direct sum would).
+template <int JM>
+__device__ void minmax_c(const AxisConst& a, const AxisTab& tab, double dk, double (&c)[JM]) {
     const int J = a.J, L = a.L;
-    double t = w / a.gam;
-    double koff = floor(t - J * 0.5);
-    double dk = t - koff;
     double s0, c0;
     sincospi(dk * a.inv_ratio, &s0, &c0);
-    // sinc values indexed by n + L + J, n = l - j in [-(L+J), L-1]
-    double sv[2 * NUFFT_MAXL + NUFFT_MAXJ + 2];
+    double r[JM];
+#pragma unroll
+    for (int j = 0; j < JM; ++j) r[j] = 0.0;
     const double pr = M_PI * a.inv_ratio;
     for (int n = -(L + J); n <= L - 1; ++n) {
         const double xn = dk + n;
         const int q = n + L + J;
-        sv[q] = (fabs(xn) < 1.0) ? sinc_direct(xn * a.inv_ratio)
-                                 : (s0 * tab.cs[q] + c0 * tab.ss[q]) * rcp_newton(pr * xn);
+        const double sv = (fabs(xn) < 1.0) ? sinc_direct(xn * a.inv_ratio)
+                                           : (s0 * tab.cs[q] + c0 * tab.ss[q]) * rcp_newton(pr * xn);
+#pragma unroll
+        for (int j = 0; j < JM; ++j) {
+            const int l = n + j + 1;
+            if (j < J && l >= -L && l <= L) r[j] += a.alpha[l < 0 ? -l : l] * sv;
+        }
     }
-    double r[NUFFT_MAXJ];
-    for (int j = 1; j <= J; ++j) {
+#pragma unroll
+    for (int j = 0; j < JM; ++j) {
         double acc = 0.0;
-        for (int l = -L; l <= L; ++l) acc += a.alpha[l < 0 ? -l : l] * sv[l - j + L + J];
-        r[j - 1] = acc;
+#pragma unroll
+        for (int i = 0; i < JM; ++i)
+            if (j < J && i < J) acc += a.T[j * J + i] * r[i];
+        c[j] = acc;
     }
+}
+
+// The coefficients depend on the point only through dk = t - koff, which
+// lies in [J/2, J/2 + 1).  They are smooth there, so they are tabulated once
+// per axis at kCTabS samples per unit of dk (plus one guard sample at each
+// end) and evaluated per point by 4-point cubic Lagrange interpolation in
+// FP64: the interpolation error, O(h^4) with h = 1/kCTabS, is below 1e-10
+// relative, far under the float32 rounding of the stored tables, at a small
+// fraction of the FP64 work of the direct sum (this GPU's FP64 rate is low).
+constexpr int kCTabS = 512;
+constexpr int kCTabN = kCTabS + 3;
+
+template <int JM>
+__global__ void ctab_kernel(const AxisConst* __restrict__ axc, const AxisTab* __restrict__ tabs,
+                            int ndim, double* __restrict__ ctab) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ndim * kCTabN) return;
+    const int d = i / kCTabN, k = i - d * kCTabN;
+    const AxisConst& a = axc[d];
+    const double dk = 0.5 * a.J + (double)(k - 1) / kCTabS;
+    double c[JM];
+    minmax_c<JM>(a, tabs[d], dk, c);
+#pragma unroll
+    for (int j = 0; j < JM; ++j) ctab[(size_t)i * JM + j] = c[j];
+}
+
+// One axis of the min-max interpolator for one point.
+//   t = om/gam, koff = floor(t - J/2), dk = t - koff, arg_j = dk - j
+//   c_j(dk) from the table (see above)
+//   u_j = exp(i gam (N-1)/2 arg_j) c_j exp(-i om N/2)            (OMEGA_u)
+//   out_j = conj(u_j)                                            (.T.conj())
+// The J phase factors come from one FP64 sincos rotated by the tabulated
+// exp(-i gam (N-1)/2 j).
+template <int JM>
+__device__ float axis_coefs(const AxisConst& a, const AxisTab& tab, const double* __restrict__ ctab,
+                            double w, float2* __restrict__ dst, int JP) {
+    const int J = a.J;
+    double t = w / a.gam;
+    double koff = floor(t - J * 0.5);
+    double dk = t - koff;
+    double u = (dk - 0.5 * J) * kCTabS;
+    int i0 = (int)floor(u);
+    i0 = min(max(i0, 0), kCTabS - 1);
+    const double f = fmin(fmax(u - i0, 0.0), 1.0);
+    // cubic Lagrange weights for samples at -1, 0, 1, 2 (table rows i0 .. i0+3)
+    const double fm1 = f - 1.0, fm2 = f - 2.0, fp1 = f + 1.0;
+    const double wa = -f * fm1 * fm2 * (1.0 / 6.0);
+    const double wb = fp1 * fm1 * fm2 * 0.5;
+    const double wc = -fp1 * f * fm2 * 0.5;
+    const double wd = fp1 * f * fm1 * (1.0 / 6.0);
+    const double* row = ctab + (size_t)i0 * JM;
     // phase of j = 1: lin*(dk - 1) - om*N/2; then rotate by exp(-i lin) per step
     double sth, cth;
     sincos(a.lin * (dk - 1.0) - w * a.half_N, &sth, &cth);
     float amax = 0.f;
-    for (int j = 0; j < J; ++j) {
-        double c = 0.0;
-        for (int i = 0; i < J; ++i) c += a.T[j * J + i] * r[i];
+#pragma unroll
+    for (int j = 0; j < JM; ++j) {
+        if (j >= J) {
+            if (j < JP) dst[j] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const double c = wa * row[j] + wb * row[JM + j] + wc * row[2 * JM + j] + wd * row[3 * JM + j];
         // exp(i th_j) with th_j = th_1 - lin*j
         const double cr = cth * tab.rc[j] + sth * tab.rs[j];
         const double ci = sth * tab.rc[j] - cth * tab.rs[j];
-        float2 v = make_float2((float)(c * cr), (float)(-c * ci));
-        out[j] = v;
+        const float2 v = make_float2((float)(c * cr), (float)(-c * ci));
+        dst[j] = v;
         amax = fmaxf(amax, sqrtf(v.x * v.x + v.y * v.y));
     }
     return amax;
 }
 
+template <int JM>
 __global__ void build_tables_kernel(const double* __restrict__ om, int64_t M, int ndim,
                                     const AxisConst* __restrict__ axc,
-                                    const AxisTab* __restrict__ tabs, Geom g,
+                                    const AxisTab* __restrict__ tabs,
+                                    const double* __restrict__ ctab, Geom g,
                                     const int* __restrict__ bin_of,
                                     const int* __restrict__ rank_of,
                                     const int* __restrict__ bin_start,
@@ -211,7 +278,6 @@ __global__ void build_tables_kernel(const double* __restrict__ om, int64_t M, in
                                     float2* __restrict__ coef0, float2* __restrict__ coef1,
                                     float2* __restrict__ coef2, float* __restrict__ wpt,
                                     unsigned int* __restrict__ wmax) {
-    float2* coefs[3] = {coef0, coef1, coef2};
     for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
          m += (int64_t)gridDim.x * blockDim.x) {
         const int bk = bin_of[m];
@@ -239,10 +305,9 @@ __global__ void build_tables_kernel(const double* __restrict__ om, int64_t M, in
             if (p >= a.K) p -= a.K;
             if (p < 0) p += a.K;
             pos[(int64_t)d * M + s] = p;
-            float2 buf[NUFFT_MAXJ];
-            float amax = axis_coefs(a, tabs[d], w, buf);
-            float2* dst = coefs[d] + s * g.JP[d];
-            for (int j = 0; j < g.JP[d]; ++j) dst[j] = (j < a.J) ? buf[j] : make_float2(0.f, 0.f);
+            float2* cd = (d == 0) ? coef0 : (d == 1) ? coef1 : coef2;
+            const float amax = axis_coefs<JM>(a, tabs[d], ctab + (size_t)d * kCTabN * JM, w,
+                                              cd + s * g.JP[d], g.JP[d]);
             wprod *= amax;
         }
         wpt[s] = wprod;
@@ -354,8 +419,12 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     int *d_bin_of = nullptr, *d_rank = nullptr, *d_cnt = nullptr, *d_start = nullptr;
     int *d_nsub = nullptr, *d_subst = nullptr, *d_err = nullptr, *d_bucket = nullptr;
     unsigned int* d_wmax = nullptr;
+    AxisTab* d_tab = nullptr;
+    double* d_ctab = nullptr;
     auto cleanup = [&]() {
         if (!om_on_device) cudaFree(d_om);
+        cudaFree(d_tab); d_tab = nullptr;
+        cudaFree(d_ctab); d_ctab = nullptr;
         cudaFree(d_bin_of); cudaFree(d_rank); cudaFree(d_cnt); cudaFree(d_start);
         cudaFree(d_nsub); cudaFree(d_subst); cudaFree(d_err); cudaFree(d_wmax);
         cudaFree(d_bucket);
@@ -412,7 +481,6 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
             htab[d].rs[j] = std::sin(a.lin * j);
         }
     }
-    AxisTab* d_tab = nullptr;
     TRY_TMP(cudaMalloc(&d_tab, sizeof(AxisTab) * 3));
     TRY_TMP(cudaMemcpyAsync(d_tab, htab, sizeof(AxisTab) * 3, cudaMemcpyHostToDevice, s));
     TRY_TMP(cudaMemcpyAsync(p->d_axc, hax, sizeof(AxisConst) * 3, cudaMemcpyHostToDevice, s));
@@ -437,9 +505,19 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     float2* c1 = c0 + (nd > 1 ? Malloc * JP[0] : 0);
     float2* c2 = c1 + (nd > 2 ? Malloc * JP[1] : 0);
     if (M > 0) {
-        build_tables_kernel<<<blocks, threads, 0, s>>>(d_om, M, nd, p->d_axc, d_tab, g, d_bin_of,
-                                                       d_rank, d_start, d_bucket, p->d_perm, p->d_pos,
-                                                       c0, c1, c2, p->d_wpt, d_wmax);
+        int jmax = 1;
+        for (int d = 0; d < nd; ++d) jmax = std::max(jmax, p->Jd[d]);
+        const int jm = (jmax <= 4) ? 4 : (jmax <= 6) ? 6 : (jmax <= 8) ? 8 : 16;
+        TRY_TMP(cudaMalloc(&d_ctab, sizeof(double) * nd * kCTabN * jm));
+        auto ckern = (jm == 4) ? ctab_kernel<4> : (jm == 6) ? ctab_kernel<6>
+                     : (jm == 8) ? ctab_kernel<8> : ctab_kernel<16>;
+        ckern<<<(nd * kCTabN + 127) / 128, 128, 0, s>>>(p->d_axc, d_tab, nd, d_ctab);
+        TRY_TMP(cudaGetLastError());
+        auto kern = (jm == 4) ? build_tables_kernel<4> : (jm == 6) ? build_tables_kernel<6>
+                    : (jm == 8) ? build_tables_kernel<8> : build_tables_kernel<16>;
+        kern<<<blocks, threads, 0, s>>>(d_om, M, nd, p->d_axc, d_tab, d_ctab, g, d_bin_of, d_rank,
+                                        d_start, d_bucket, p->d_perm, p->d_pos, c0, c1, c2, p->d_wpt,
+                                        d_wmax);
         TRY_TMP(cudaGetLastError());
     }
     const int bblocks = (int)std::min<int64_t>((nbins + threads - 1) / threads, 65535);
@@ -453,7 +531,8 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     TRY_TMP(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     TRY_TMP(cudaMemcpyAsync(&h_wmax, d_wmax, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
     TRY_TMP(cudaStreamSynchronize(s));
-    cudaFree(d_tab);
+    cudaFree(d_tab); d_tab = nullptr;
+    cudaFree(d_ctab); d_ctab = nullptr;
     if (h_err) {
         cleanup();
         free_points(p);
