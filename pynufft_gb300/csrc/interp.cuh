@@ -542,7 +542,7 @@ __device__ __forceinline__ int tile_addr(const int (&t)[3], const TileStrides& t
 // bounded wait sets the plan's error flag and returns if the copies never
 // land.  Otherwise every thread loads cells through registers.
 template <int DIM, int JM, bool EX, bool BULK>
-__global__ void __launch_bounds__(128) k2y_spoint_kernel(Geom g, const float2* __restrict__ grid,
+__global__ void __launch_bounds__(256) k2y_spoint_kernel(Geom g, const float2* __restrict__ grid,
                                                          float2* __restrict__ y) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* tile = reinterpret_cast<float2*>(smem_raw);
@@ -691,7 +691,7 @@ template <> struct Acc<true> {
 };
 
 // Per-coil fixed-point scales of one sub-problem (fast mode), written to
-// scale[0..bcur).  Requires a block-wide barrier afterwards.
+// scale[0..bcur); ends with a block-wide barrier.
 __device__ __forceinline__ void subproblem_scales(const Geom& g, const int4& sp, const float2* y,
                                                   int b0, int bcur, float* bound, float* scale) {
     for (int b = threadIdx.x; b < bcur; b += blockDim.x) bound[b] = 0.f;
@@ -709,11 +709,11 @@ __device__ __forceinline__ void subproblem_scales(const Geom& g, const int4& sp,
     }
     __syncthreads();
     for (int b = threadIdx.x; b < bcur; b += blockDim.x) {
-        // |sum of any cell| <= bound < 2^e, so a scale of 2^(30-e) keeps it < 2^30
-        int e = 0;
-        const float bb = bound[b] * 1.001f;
-        if (bb > 0.f && isfinite(bb)) frexpf(bb, &e);
-        scale[b] = ldexpf(1.f, 30 - e);
+        // |sum of any cell| <= bound, so a scale of 2e9 / bound keeps every
+        // partial sum below 2e9 < 2^31; the 7% left covers the rounding of the
+        // contributions (half a unit each).  Clamped for vanishing bounds.
+        const float bb = bound[b];
+        scale[b] = (bb > 0.f && isfinite(bb)) ? fminf(2.0e9f / bb, 1.0e30f) : 1.0f;
     }
     __syncthreads();
 }
@@ -969,7 +969,7 @@ __device__ __forceinline__ void add_row(unsigned* re, unsigned* im, int c, float
 }
 
 template <int DIM, int JM, bool EX>
-__global__ void __launch_bounds__(128) y2k_spoint_kernel(Geom g, const float2* __restrict__ y,
+__global__ void __launch_bounds__(256) y2k_spoint_kernel(Geom g, const float2* __restrict__ y,
                                                          float2* __restrict__ grid) {
     static_assert(DIM > 1, "paired gridding splits an outer axis");
     extern __shared__ __align__(16) unsigned char smem_raw[];

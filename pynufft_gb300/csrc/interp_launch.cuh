@@ -9,6 +9,12 @@
 
 namespace nufft {
 
+// Threads per block of the paired kernels: two per point of an average
+// sub-problem, 128 or 256.
+inline int paired_threads(const Geom& g) {
+    return (g.nsub > 0 && g.M > 96 * g.nsub) ? 256 : 128;
+}
+
 inline int pick_team(int B) {
     if (B >= 32) return 32;
     if (B >= 8) return 8;
@@ -43,7 +49,7 @@ static void k2y_launch(const Geom& g, const float2* grid, float2* y, cudaStream_
                 else
                     kern = exact ? k2y_spoint_kernel<DIM, JM, true, false>
                                  : k2y_spoint_kernel<DIM, JM, false, false>;
-                nt = 128;
+                nt = paired_threads(g);
             }
             if (smem > 48 * 1024)
                 cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -137,7 +143,7 @@ static int y2k_launch(const Geom& g, const float2* y, float2* grid, unsigned lon
                     return NUFFT_ECUDA;
                 }
             }
-            if (g.nsub > 0) pk<<<(unsigned)g.nsub, 128, psmem, s>>>(g, y, grid);
+            if (g.nsub > 0) pk<<<(unsigned)g.nsub, paired_threads(g), psmem, s>>>(g, y, grid);
             return check_launch("y2k_spoint_kernel");
         }
     }

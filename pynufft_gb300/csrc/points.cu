@@ -353,13 +353,16 @@ void free_points(nufft_plan_s* p) {
 
 static void default_bins(const nufft_plan_s* p, int bs[3], int& maxsub) {
     // cells per bin axis; the gridding tile is (bs + J - 1) per axis.  Sub-
-    // problems hold at most 256 points, which keeps the 32-bit fixed-point
-    // rounding unit of the fast gridding mode below float32 resolution.
+    // problems hold at most 256 points (512 for the single-coil 3D bins, whose
+    // 256-thread paired kernels take 128 points per pass), which keeps the
+    // 32-bit fixed-point rounding of the fast gridding mode near float32
+    // resolution (measured 5e-7 relative L2 against the exact mode).
     for (int d = 0; d < 3; ++d) bs[d] = 1;
+    maxsub = 256;
     if (p->ndim == 1) { bs[0] = 1024; }
     else if (p->ndim == 2) { bs[0] = bs[1] = (p->B >= 8) ? 16 : 32; }
-    else { bs[0] = bs[1] = 8; bs[2] = (p->B >= 8) ? 4 : 16; }
-    maxsub = 256;
+    else if (p->B >= 8) { bs[0] = bs[1] = 8; bs[2] = 4; }
+    else { bs[0] = 8; bs[1] = bs[2] = 16; maxsub = 512; }
     for (int d = 0; d < p->ndim; ++d) {
         if (p->user_bs[d] > 0) bs[d] = p->user_bs[d];
         bs[d] = std::min(bs[d], p->Kd[d]);
