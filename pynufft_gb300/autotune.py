@@ -23,7 +23,7 @@ CACHE = os.environ.get('PYNUFFT_GB300_TUNE_CACHE',
 BIN_CANDIDATES = {
     1: [(512,), (1024,), (2048,)],
     2: [(16, 16), (32, 32), (32, 64), (64, 64)],
-    3: [(4, 8, 8), (8, 8, 8), (8, 8, 16), (16, 16, 16)],
+    3: [(8, 8, 8), (8, 8, 16), (8, 16, 16), (16, 16, 16)],
 }
 SUB_CANDIDATES = [128, 256, 512]
 K2Y = ['tile', 'tile_point', 'zteam', 'point']

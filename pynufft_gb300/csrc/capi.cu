@@ -302,9 +302,7 @@ int nufft_xx2x(nufft_plan_t p, const void* xx, void* x, void* stream) {
 int nufft_xx2k(nufft_plan_t p, const void* xx, void* k, void* stream) {
     NUFFT_TRY(need_plan(p, "nufft_xx2k"));
     NUFFT_TRY(need_ptrs(xx, k, "nufft_xx2k"));
-    cudaStream_t s = as_stream(stream);
-    NUFFT_TRY(launch_pad(p, (const float2*)xx, (float2*)k, false, -1, s));
-    return fft_exec(p, (float2*)k, -1, s);
+    return forward_from_image(p, (const float2*)xx, false, (float2*)k, as_stream(stream));
 }
 
 int nufft_k2xx(nufft_plan_t p, const void* k, void* xx, void* stream) {
@@ -333,8 +331,7 @@ int nufft_forward(nufft_plan_t p, const void* x, void* y, void* stream) {
     NUFFT_TRY(need_points(p, "nufft_forward"));
     NUFFT_TRY(need_ptrs(x, y, "nufft_forward", p));
     cudaStream_t s = as_stream(stream);
-    NUFFT_TRY(launch_pad(p, (const float2*)x, p->d_grid, true, -1, s));
-    NUFFT_TRY(fft_exec(p, p->d_grid, -1, s));
+    NUFFT_TRY(forward_from_image(p, (const float2*)x, true, p->d_grid, s));
     return launch_k2y(p, p->d_grid, (float2*)y, s);
 }
 

@@ -150,6 +150,36 @@ __global__ void pad_rows_kernel(ImgGeom g, const float2* __restrict__ xx, float2
   }
 }
 
+// Nd corner only: grid row (inst, n0[, n1]) first N cells = x row (* sn);
+// every other cell of `grid` is left as it is (zero in the plan's padded
+// input buffer, which nothing else writes).  One coil.
+template <int DIM>
+__global__ void corner_rows_kernel(ImgGeom g, const float2* __restrict__ xx, float2* __restrict__ grid,
+                                   int apply_sn, int64_t rows) {
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    int64_t inst;
+    int n[3] = {0, 0, 0};
+    row_index<DIM>(r, g.N[0], g.N[1], inst, n[0], n[1]);
+    constexpr int last = DIM - 1;
+    const int KL = g.K[last], NL = g.N[last];
+    int64_t grow = inst;
+    if (DIM >= 2) grow = grow * g.K[0] + n[0];
+    if (DIM == 3) grow = grow * g.K[1] + n[1];
+    const float2* src = xx + (size_t)r * NL;
+    float2* dst = grid + (size_t)grow * KL;
+    const float s_lead = apply_sn ? lead_sn<DIM>(g.sn[0], g.sn[1], n[0], n[1]) : 1.f;
+    for (int k = threadIdx.x; k < NL; k += blockDim.x) {
+        float2 v = __ldg(src + k);
+        if (apply_sn) {
+            const float sc = s_lead * __ldg(g.sn[last] + k);
+            v.x *= sc;
+            v.y *= sc;
+        }
+        dst[k] = v;
+    }
+  }
+}
+
 // x row = grid row (first N of the last axis) / prod(Kd) * (sn if apply_sn) / (sn if divide_sn)
 template <int DIM>
 __global__ void crop_rows_kernel(ImgGeom g, const float2* __restrict__ grid, float2* __restrict__ xx,
@@ -304,6 +334,39 @@ int launch_pad(const nufft_plan_s* p, const float2* xx, float2* grid, bool apply
     return check_launch("pad_rows_kernel");
 }
 
+// Image (Nd, caller's layout) -> oversampled spectrum k: zero-pad (x sn when
+// apply_sn) and forward FFT.  For one coil and one instance the pad only
+// writes the Nd corner of the plan's padded input buffer (its zeros are
+// never overwritten), the (y[,z]) FFTs run out of place on its first Nd[0]
+// slabs into the slab buffer (whose other slabs stay zero), and the x-axis
+// FFTs write k: the 134 MB zero fill of a 256^3 grid is not rewritten on
+// every call.
+int forward_from_image(nufft_plan_s* p, const float2* xx, bool apply_sn, float2* k,
+                       cudaStream_t s) {
+    if (!(p->fft_pruned && p->d_padin)) {
+        NUFFT_TRY(launch_pad(p, xx, k, apply_sn, -1, s));
+        return fft_exec(p, k, -1, s);
+    }
+    ImgGeom g = img_geom(p);
+    const int64_t rows = rows_of(g, g.N, 1);
+    const unsigned nb = row_blocks(p, rows);
+    const int nt = row_threads(g.N[g.ndim - 1]);
+    const int as = apply_sn ? 1 : 0;
+    if (p->ndim == 2)
+        corner_rows_kernel<2><<<nb, nt, 0, s>>>(g, xx, p->d_padin, as, rows);
+    else
+        corner_rows_kernel<3><<<nb, nt, 0, s>>>(g, xx, p->d_padin, as, rows);
+    NUFFT_TRY(check_launch("corner_rows_kernel"));
+    cufftComplex* a = reinterpret_cast<cufftComplex*>(p->d_padin);
+    cufftComplex* b = reinterpret_cast<cufftComplex*>(p->d_slabout);
+    cufftComplex* kc = reinterpret_cast<cufftComplex*>(k);
+    NUFFT_CUFFT_TRY(cufftSetStream(p->fft_slab, s));
+    NUFFT_CUFFT_TRY(cufftSetStream(p->fft_x, s));
+    NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_slab, a, b, CUFFT_FORWARD));
+    NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_x, b, kc, CUFFT_FORWARD));
+    return NUFFT_OK;
+}
+
 int launch_crop(const nufft_plan_s* p, const float2* grid, float2* xx, bool apply_sn,
                 bool divide_sn, cudaStream_t s) {
     ImgGeom g = img_geom(p);
@@ -384,6 +447,15 @@ int fft_init(nufft_plan_s* p) {
         NUFFT_CUDA_TRY(cudaMalloc(&p->d_fftwork, work));
         p->dev_bytes += work;
     }
+    if (p->fft_pruned) {
+        // padded input (first Nd[0] slabs) and slab-FFT output, zero once
+        const size_t nin = (size_t)p->Nd[0] * (p->prodK / p->Kd[0]);
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_padin, sizeof(float2) * nin));
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_slabout, sizeof(float2) * p->prodK));
+        NUFFT_CUDA_TRY(cudaMemset(p->d_padin, 0, sizeof(float2) * nin));
+        NUFFT_CUDA_TRY(cudaMemset(p->d_slabout, 0, sizeof(float2) * p->prodK));
+        p->dev_bytes += sizeof(float2) * (nin + p->prodK);
+    }
     NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft, p->d_fftwork));
     if (p->fft_pruned) {
         NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_slab, p->d_fftwork));
@@ -401,6 +473,9 @@ void fft_destroy(nufft_plan_s* p) {
     p->fft_ok = p->fft_pruned = false;
     cudaFree(p->d_fftwork);
     p->d_fftwork = nullptr;
+    cudaFree(p->d_padin);
+    cudaFree(p->d_slabout);
+    p->d_padin = p->d_slabout = nullptr;
 }
 
 // direction < 0: forward (numpy fftn sign); > 0: inverse, unnormalised.

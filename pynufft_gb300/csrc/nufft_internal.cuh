@@ -147,6 +147,8 @@ struct nufft_plan_s {
     cufftHandle fft_x = 0;            // x-axis FFTs over all slabs
     bool fft_ok = false, fft_pruned = false;
     void* d_fftwork = nullptr;        // shared cuFFT work area
+    float2* d_padin = nullptr;        // pruned forward: zero-padded input, first Nd[0] slabs
+    float2* d_slabout = nullptr;      // pruned forward: slab-FFT output, other slabs zero
     size_t dev_bytes = 0;
 
     nufft::Geom geom() const;
@@ -205,6 +207,8 @@ int launch_pad(const nufft_plan_s* p, const float2* xx, float2* grid, bool apply
 int launch_crop(const nufft_plan_s* p, const float2* grid, float2* xx, bool apply_sn,
                 bool divide_sn, cudaStream_t s);
 int fft_exec(nufft_plan_s* p, float2* grid, int direction, cudaStream_t s);
+int forward_from_image(nufft_plan_s* p, const float2* xx, bool apply_sn, float2* k,
+                       cudaStream_t s);
 int launch_pad_sense(const nufft_plan_s* p, const float2* x, float2* grid, cudaStream_t s);
 int launch_crop_sense(const nufft_plan_s* p, const float2* grid, float2* x, cudaStream_t s);
 int fft_init(nufft_plan_s* p);

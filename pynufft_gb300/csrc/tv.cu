@@ -187,8 +187,7 @@ int solve_l1tvols(nufft_plan_s* p, const float2* y, float2* x, int maxiter, doub
         fill_ones_kernel<<<grid_for(p, p->M), 256, 0, s>>>(p->d_ybuf, p->M);
         NUFFT_CUDA_TRY(cudaGetLastError());
         NUFFT_TRY(nufft_adjoint(p, p->d_ybuf, aha, s));
-        NUFFT_TRY(launch_pad(p, aha, p->d_grid, false, -1, s));
-        NUFFT_TRY(fft_exec(p, p->d_grid, -1, s));
+        NUFFT_TRY(forward_from_image(p, aha, false, p->d_grid, s));
         tv_uker_kernel<<<grid_for(p, nk), 256, 0, s>>>(p->d_grid, uker, d.ndim, p->Kd[0], p->Kd[1],
                                                        p->Kd[2], nk, mu, lmbd);
         NUFFT_CUDA_TRY(cudaGetLastError());
@@ -197,8 +196,7 @@ int solve_l1tvols(nufft_plan_s* p, const float2* y, float2* x, int maxiter, doub
         for (int it = 0; it < maxiter; ++it) {
             tv_rhs_kernel<<<gi, 256, 0, s>>>(d, ahyk, dd, bb, rhs, mu, lmbd);
             NUFFT_CUDA_TRY(cudaGetLastError());
-            NUFFT_TRY(launch_pad(p, rhs, p->d_grid, false, -1, s));
-            NUFFT_TRY(fft_exec(p, p->d_grid, -1, s));
+            NUFFT_TRY(forward_from_image(p, rhs, false, p->d_grid, s));
             tv_kdiv_kernel<<<gk, 256, 0, s>>>(p->d_grid, uker, nk);
             NUFFT_CUDA_TRY(cudaGetLastError());
             NUFFT_TRY(fft_exec(p, p->d_grid, +1, s));
