@@ -149,6 +149,7 @@ struct nufft_plan_s {
     void* d_fftwork = nullptr;        // shared cuFFT work area
     float2* d_padin = nullptr;        // pruned forward: zero-padded input, first Nd[0] slabs
     float2* d_slabout = nullptr;      // pruned forward: slab-FFT output, other slabs zero
+    float2* d_cm = nullptr;           // B > 1: coil-major copy of the grid for the FFTs
     size_t dev_bytes = 0;
 
     nufft::Geom geom() const;
