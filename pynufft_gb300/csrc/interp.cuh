@@ -985,7 +985,10 @@ __global__ void __launch_bounds__(256) y2k_spoint_kernel(Geom g, const float2* _
     const int Jz = EX ? JM : g.J[DI];
     unsigned* re = reinterpret_cast<unsigned*>(smem_raw);
     unsigned* im = re + ts.n;
-    for (int e = threadIdx.x; e < 2 * ts.n; e += blockDim.x) re[e] = 0u;
+    {   // zero both planes, 16 bytes per store (2 n is a multiple of 4)
+        uint4* z4 = reinterpret_cast<uint4*>(smem_raw);
+        for (int e = threadIdx.x; e < ts.n / 2; e += blockDim.x) z4[e] = make_uint4(0u, 0u, 0u, 0u);
+    }
     subproblem_scales(g, sp, y, 0, 1, s_bound, s_scale);   // ends with a barrier
     const float sc = s_scale[0];
     const int lane = threadIdx.x & 31;
