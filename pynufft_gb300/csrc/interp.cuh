@@ -730,22 +730,36 @@ __device__ __forceinline__ void flush_tile(const Geom& g, const int (&o)[3], int
     const int nsm = ncell * bcur;
     const size_t ibase = (size_t)inst * g.prodK;
     const int B = g.B;
-    for (int b = 0; b < bcur; ++b) {
+    auto put = [&](int e, size_t gi, float inv) {
+        const typename Acc<DET>::T vx = tile[e], vy = tile[nsm + e];
+        if (vx == 0 && vy == 0) return;
+        if constexpr (DET) {
+            if (vx) atomicAdd(igrid + 2 * gi, (unsigned long long)vx);
+            if (vy) atomicAdd(igrid + 2 * gi + 1, (unsigned long long)vy);
+        } else {
+            atomicAdd(grid + gi, make_float2(__int2float_rn((int)vx) * inv,
+                                             __int2float_rn((int)vy) * inv));
+        }
+    };
+    if constexpr (CELL_MAJOR) {
+        // threads split as (cell, coil), coil fastest (bcur <= blockDim): a
+        // warp reads consecutive words of the tile and adds to consecutive
+        // coils of the grid
+        const int cpb = (int)blockDim.x / bcur;   // cells per pass
+        const int b = (int)threadIdx.x % bcur, c0 = (int)threadIdx.x / bcur;
+        if (c0 >= cpb) return;
         const float inv = DET ? 1.f : 1.f / scale[b];
         TileWalk<DIM> w;
-        w.init(g.T, threadIdx.x, blockDim.x);
-        for (int c = threadIdx.x; c < ncell; c += blockDim.x, w.next()) {
-            const int e = CELL_MAJOR ? c * bcur + b : b * ncell + c;
-            const typename Acc<DET>::T vx = tile[e], vy = tile[nsm + e];
-            if (vx == 0 && vy == 0) continue;
-            const size_t gi = (ibase + w.cell(g, o)) * B + b0 + b;
-            if constexpr (DET) {
-                if (vx) atomicAdd(igrid + 2 * gi, (unsigned long long)vx);
-                if (vy) atomicAdd(igrid + 2 * gi + 1, (unsigned long long)vy);
-            } else {
-                atomicAdd(grid + gi, make_float2(__int2float_rn((int)vx) * inv,
-                                                 __int2float_rn((int)vy) * inv));
-            }
+        w.init(g.T, c0, cpb);
+        for (int c = c0; c < ncell; c += cpb, w.next())
+            put(c * bcur + b, (ibase + w.cell(g, o)) * B + b0 + b, inv);
+    } else {
+        for (int b = 0; b < bcur; ++b) {
+            const float inv = DET ? 1.f : 1.f / scale[b];
+            TileWalk<DIM> w;
+            w.init(g.T, threadIdx.x, blockDim.x);
+            for (int c = threadIdx.x; c < ncell; c += blockDim.x, w.next())
+                put(b * ncell + c, (ibase + w.cell(g, o)) * B + b0 + b, inv);
         }
     }
 }

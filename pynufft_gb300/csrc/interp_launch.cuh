@@ -94,10 +94,10 @@ static void k2y_jm(int jm, const Geom& g, const float2* grid, float2* y, cudaStr
 // ---------------------------------------------------------------------------
 // y2k
 // ---------------------------------------------------------------------------
-// Coils per shared-memory chunk: as many as fit in ~100 KB (two blocks per
+// Coils per shared-memory chunk: as many as fit in 112 KB (two blocks per
 // SM), split into equal chunks, at most 64; one coil may use up to 200 KB.
 inline int coil_chunk(size_t cellbytes, int B, size_t* smem) {
-    const size_t target = 100 * 1024, big = 200 * 1024;
+    const size_t target = 112 * 1024, big = 200 * 1024;
     if (cellbytes > big) return 0;
     int bmax = (int)std::min<size_t>(64, std::max<size_t>(1, target / cellbytes));
     const int n = (B + bmax - 1) / bmax;
