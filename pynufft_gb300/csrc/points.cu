@@ -83,12 +83,22 @@ __global__ void bin_points_kernel(const double* __restrict__ om, int64_t M, int 
             continue;
         }
         bin += (int64_t)inst * g.nbin_inst;
-        // bank key: the point's first footprint cell in the padded tile
-        // layout, modulo the bank buckets of the dimension
-        const TileStrides ts = tile_strides(ndim, g.T);
-        const int addr = (ndim == 3) ? lp[0] * ts.sx + lp[1] * ts.sy + lp[2]
-                         : (ndim == 2) ? lp[0] * ts.sy + lp[1] : lp[0];
-        const int key = addr & (bank_keys(ndim) - 1);
+        // bank key: the point's first footprint cell in the tile layout of
+        // its gridding kernel, modulo the points that share a warp there
+        int key;
+        if (g.B >= 8) {
+            // coil teams of G lanes, cell-major tile with the coils fastest:
+            // 32 / G points per warp, banks set by the flat cell mod 32 / G
+            const int G = (g.B >= 32) ? 32 : 8;
+            int flat = lp[0];
+            for (int d = 1; d < ndim; ++d) flat = flat * g.T[d] + lp[d];
+            key = flat % (32 / G);
+        } else {
+            const TileStrides ts = tile_strides(ndim, g.T);
+            const int addr = (ndim == 3) ? lp[0] * ts.sx + lp[1] * ts.sy + lp[2]
+                             : (ndim == 2) ? lp[0] * ts.sy + lp[1] : lp[0];
+            key = addr & (bank_keys(ndim) - 1);
+        }
         bin_of[m] = (int)(bin * 32 + key);
         rank_of[m] = atomicAdd(&bucket_count[bin * 32 + key], 1);
     }
