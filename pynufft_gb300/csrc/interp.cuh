@@ -1071,7 +1071,7 @@ __global__ void __launch_bounds__(256) y2k_spoint_kernel(Geom g, const float2* _
 // ---------------------------------------------------------------------------
 // y2k, coil-teams (B >= 8): tile layout cell-major, coil fastest
 // ---------------------------------------------------------------------------
-template <int DIM, int JM, int G, bool DET>
+template <int DIM, int JM, int G, bool DET, bool EX>
 __global__ void __launch_bounds__(256) y2k_coil_kernel(Geom g, const float2* __restrict__ y,
                                                        float2* __restrict__ grid,
                                                        unsigned long long* __restrict__ igrid,
@@ -1092,7 +1092,9 @@ __global__ void __launch_bounds__(256) y2k_coil_kernel(Geom g, const float2* __r
     for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
     const int B = g.B;
     const int team = threadIdx.x / G, lane = threadIdx.x % G, nteam = blockDim.x / G;
-    const int J0 = g.J[0];
+    const int J0 = EX ? JM : g.J[0];
+    const int Jy = EX ? JM : g.J[DY];
+    const int Jz = EX ? JM : g.J[DI];
     T* tile = reinterpret_cast<T*>(smem_raw);
 
     for (int b0 = 0; b0 < B; b0 += bc) {
@@ -1108,10 +1110,19 @@ __global__ void __launch_bounds__(256) y2k_coil_kernel(Geom g, const float2* __r
         T* re = tile;
         T* im = tile + nsm;
         for (int s = sp.y + team; s < sp.y + sp.z; s += nteam) {
-            int iz[JM], iy[JM];
             float2 cz[JM], cy[JM];
-            load_axis<JM>(g, DI, s, iz, cz);
-            if constexpr (DIM > 1) load_axis<JM>(g, DY, s, iy, cy);
+            {
+                const float2* src = g.coef[DI] + (size_t)s * g.JP[DI];
+#pragma unroll
+                for (int k = 0; k < JM; ++k)
+                    cz[k] = (EX || k < Jz) ? __ldg(src + k) : make_float2(0.f, 0.f);
+            }
+            if constexpr (DIM > 1) {
+                const float2* src = g.coef[DY] + (size_t)s * g.JP[DY];
+#pragma unroll
+                for (int j = 0; j < JM; ++j)
+                    cy[j] = (EX || j < Jy) ? __ldg(src + j) : make_float2(0.f, 0.f);
+            }
             const int lz = __ldg(g.pos[DI] + s) - o[DI];
             const int ly = (DIM > 1) ? __ldg(g.pos[DY] + s) - o[DY] : 0;
             const int lx = (DIM > 2) ? __ldg(g.pos[0] + s) - o[0] : 0;
@@ -1129,16 +1140,17 @@ __global__ void __launch_bounds__(256) y2k_coil_kernel(Geom g, const float2* __r
                     const int ci = (DIM > 2) ? (lx + i) * Ty : 0;
 #pragma unroll
                     for (int j = 0; j < ((DIM > 1) ? JM : 1); ++j) {
-                        if (DIM > 1 && j >= g.J[DY]) continue;
+                        if (!EX && DIM > 1 && j >= Jy) continue;
                         const float2 wij = (DIM > 1) ? cmulc(wi, cy[j]) : wi;
                         const int cj = (DIM > 1) ? (ci + ly + j) * Tz + lz : lz;
+                        T* rr = re + cj * bcur + b;
+                        T* ii = im + cj * bcur + b;
 #pragma unroll
                         for (int kk = 0; kk < JM; ++kk) {
-                            if (kk >= g.J[DI]) continue;
+                            if (!EX && kk >= Jz) continue;
                             const float2 w = cmulc(wij, cz[kk]);
-                            const int e = (cj + kk) * bcur + b;
-                            atomicAdd(re + e, Acc<DET>::fix(w.x, 1.f));
-                            atomicAdd(im + e, Acc<DET>::fix(w.y, 1.f));
+                            atomicAdd(rr + kk * bcur, Acc<DET>::fix(w.x, 1.f));
+                            atomicAdd(ii + kk * bcur, Acc<DET>::fix(w.y, 1.f));
                         }
                     }
                 }

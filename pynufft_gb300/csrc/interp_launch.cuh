@@ -159,7 +159,9 @@ static int y2k_launch(const Geom& g, const float2* y, float2* grid, unsigned lon
             kern = y2k_zteam_kernel<DIM, JM, DET>;
         }
     } else {
-        kern = y2k_coil_kernel<DIM, JM, G, DET>;
+        bool exact = true;
+        for (int d = 0; d < DIM; ++d) exact = exact && (g.J[d] == JM);
+        kern = exact ? y2k_coil_kernel<DIM, JM, G, DET, true> : y2k_coil_kernel<DIM, JM, G, DET, false>;
     }
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
