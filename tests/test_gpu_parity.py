@@ -349,3 +349,31 @@ def test_interpolator_tables_at_float_precision(NUFFT, case):
     A = NUFFT(0)
     A.plan(g['om'], _tup(g['Nd']), _tup(g['Kd']), _tup(g['Jd']))
     assert rel_l2(A.k2y(g['k']), g['k2y']) < 1e-6
+
+
+def test_cg_on_many_instances_and_coils_matches_oracle(NUFFT):
+    """solve(y, 'cg') on a plan of several instances and coils runs one
+    independent CG system per (instance, coil), with its own scalars and its
+    own stopping test: each matches the oracle's CG on that instance and coil,
+    and an all-zero system stops at once with x = 0."""
+    rng = np.random.default_rng(31)
+    Nd, Kd, Jd, B = (16, 18), (32, 36), (6, 6), 2
+    Ms = [700, 1100, 400]
+    oms = [rng.uniform(-np.pi, np.pi, (m, 2)) for m in Ms]
+    A = NUFFT(0)
+    A.plan_many(oms, Nd, Kd, Jd, batch=B)
+    y = cplx(rng, (sum(Ms), B))
+    y[Ms[0]:Ms[0] + Ms[1], 1] = 0          # instance 1, coil 1: b = 0
+    x, it = A.solve(y, 'cg', maxiter=4, return_info=True)
+    assert it == 4 and x.shape == (3,) + Nd + (B,)
+    off = 0
+    for i, om in enumerate(oms):
+        O = OracleNUFFT()
+        O.plan(om, Nd, Kd, Jd, batch=B)
+        xo = O.solve(y[off:off + Ms[i]], 'cg', maxiter=4)
+        for b in range(B):
+            if i == 1 and b == 1:
+                assert not np.any(x[i][..., b])
+            else:
+                assert rel_l2(x[i][..., b], xo[..., b]) < 1e-4
+        off += Ms[i]
