@@ -676,6 +676,116 @@ __global__ void __launch_bounds__(256) k2y_spoint_kernel(Geom g, const float2* _
 }
 
 // ---------------------------------------------------------------------------
+// k2y, coil teams on a shared tile (2D/3D, an even number of coils): the
+// block stages its sub-problem's footprint for all coils in shared memory --
+// each tile row, Tz cells x B coils, is contiguous in the coil-fastest grid
+// and arrives by one or two bulk copies (two where it wraps around the
+// periodic grid) -- and teams of G lanes (one point each, lanes over coils)
+// gather from it.  Every grid cell of a bin is read from memory once instead
+// of once per point that covers it.  EX: every axis has exactly JM taps.
+// ---------------------------------------------------------------------------
+template <int DIM, int JM, int G, bool EX>
+__global__ void __launch_bounds__(256) k2y_ctile_kernel(Geom g, const float2* __restrict__ grid,
+                                                        float2* __restrict__ y) {
+    static_assert(DIM > 1, "tiles of rows");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t s_bar;
+    float2* tile = reinterpret_cast<float2*>(smem_raw);
+    const int4 sp = g.sub[blockIdx.x];
+    int o[3];
+    tile_origin<DIM>(g, sp, o);
+    constexpr int DI = DIM - 1;
+    constexpr int DY = DIM - 2;
+    const int B = g.B;
+    const int Tz = g.T[DI], Ty = g.T[DY];
+    const int rowB = Tz * B;                       // elements per tile row
+    const int nrows = (DIM == 3) ? g.T[0] * g.T[1] : g.T[0];
+    const size_t ibase = (size_t)sp.w * g.prodK;
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar, 1);
+        mbar_arrive_expect_tx(&s_bar, (uint32_t)(nrows * rowB) * 8u);
+    }
+    __syncthreads();
+    const int Kz = g.K[DI], oz = o[DI];
+    const int n1 = min(Tz, Kz - oz);
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+        size_t rowcell;
+        if constexpr (DIM == 3) {
+            const int rx = r / g.T[1], ry = r - rx * g.T[1];
+            rowcell = ((size_t)wrapn(o[0] + rx, g.K[0]) * g.K[1] + wrapn(o[1] + ry, g.K[1])) * Kz;
+        } else {
+            rowcell = (size_t)wrapn(o[0] + r, g.K[0]) * Kz;
+        }
+        float2* dst = tile + (size_t)r * rowB;
+        const float2* src = grid + (ibase + rowcell) * B;
+        bulk_g2s(dst, src + (size_t)oz * B, (uint32_t)(n1 * B) * 8u, &s_bar);
+        if (n1 < Tz) bulk_g2s(dst + n1 * B, src, (uint32_t)((Tz - n1) * B) * 8u, &s_bar);
+    }
+    const bool ok = mbar_wait_bounded(&s_bar, 0);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicExch(g.kerr, 1);
+        mbar_wait_bounded(&s_bar, 0);   // a second bound for copies still in flight
+        return;
+    }
+    const int J0 = EX ? JM : g.J[0];
+    const int Jy = EX ? JM : g.J[DY];
+    const int Jz = EX ? JM : g.J[DI];
+    const int team = threadIdx.x / G, lane = threadIdx.x % G, nteam = blockDim.x / G;
+    for (int s = sp.y + team; s < sp.y + sp.z; s += nteam) {
+        float2 cz[JM], cy[JM];
+        {
+            const float2* src = g.coef[DI] + (size_t)s * g.JP[DI];
+#pragma unroll
+            for (int k = 0; k < JM; ++k)
+                cz[k] = (EX || k < Jz) ? __ldg(src + k) : make_float2(0.f, 0.f);
+            const float2* srcy = g.coef[DY] + (size_t)s * g.JP[DY];
+#pragma unroll
+            for (int j = 0; j < JM; ++j)
+                cy[j] = (EX || j < Jy) ? __ldg(srcy + j) : make_float2(0.f, 0.f);
+        }
+        const int lz = __ldg(g.pos[DI] + s) - o[DI];
+        const int ly = __ldg(g.pos[DY] + s) - o[DY];
+        const int lx = (DIM == 3) ? __ldg(g.pos[0] + s) - o[0] : 0;
+        const float2* c0src = g.coef[0] + (size_t)s * g.JP[0];
+        const int m = __ldg(g.perm + s);
+        for (int b = lane; b < B; b += G) {
+            float2 acc = make_float2(0.f, 0.f);
+            const float2* tb = tile + lz * B + b;
+            if constexpr (DIM == 2) {
+#pragma unroll
+                for (int j = 0; j < JM; ++j) {
+                    if (!EX && j >= Jy) continue;
+                    const float2* row = tb + (ly + j) * rowB;
+                    float2 t = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int k = 0; k < JM; ++k)
+                        if (EX || k < Jz) cfma(t, cz[k], row[k * B]);
+                    cfma(acc, cy[j], t);
+                }
+            } else {
+#pragma unroll 1
+                for (int i = 0; i < J0; ++i) {
+                    const float2* pl = tb + ((lx + i) * Ty + ly) * rowB;
+                    float2 ti = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int j = 0; j < JM; ++j) {
+                        if (!EX && j >= Jy) continue;
+                        const float2* row = pl + j * rowB;
+                        float2 t = make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int k = 0; k < JM; ++k)
+                            if (EX || k < Jz) cfma(t, cz[k], row[k * B]);
+                        cfma(ti, cy[j], t);
+                    }
+                    cfma(acc, __ldg(c0src + i), ti);
+                }
+            }
+            y[(size_t)m * B + b] = acc;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // y2k shared pieces
 // ---------------------------------------------------------------------------
 // Fixed-point accumulator types: 32-bit with a per-sub-problem scale (fast

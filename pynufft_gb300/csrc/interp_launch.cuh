@@ -67,6 +67,24 @@ static void k2y_launch(const Geom& g, const float2* grid, float2* y, cudaStream_
             k2y_zteam_kernel<DIM, JM><<<(unsigned)blocks, threads, 0, s>>>(g, grid, y);
         }
     } else {
+        if constexpr (DIM > 1) {
+            // coil teams on a shared tile when the tile of all coils fits two
+            // blocks per SM and rows are whole 16-byte units (even B)
+            int ncell = 1;
+            for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
+            const size_t smem = sizeof(float2) * (size_t)ncell * g.B;
+            if (g.B % 2 == 0 && smem <= 112 * 1024 && g.nsub > 0 &&
+                (reinterpret_cast<uintptr_t>(grid) & 15) == 0 && g.T[DIM - 1] <= g.K[DIM - 1]) {
+                bool exact = true;
+                for (int d = 0; d < DIM; ++d) exact = exact && (g.J[d] == JM);
+                void (*kern)(Geom, const float2*, float2*) =
+                    exact ? k2y_ctile_kernel<DIM, JM, G, true> : k2y_ctile_kernel<DIM, JM, G, false>;
+                if (smem > 48 * 1024)
+                    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                kern<<<(unsigned)g.nsub, threads, smem, s>>>(g, grid, y);
+                return;
+            }
+        }
         const int64_t blocks = (g.M * G + threads - 1) / threads;
         k2y_coil_kernel<DIM, JM, G><<<(unsigned)blocks, threads, 0, s>>>(g, grid, y);
     }
