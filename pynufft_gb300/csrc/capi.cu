@@ -309,6 +309,7 @@ int nufft_k2xx(nufft_plan_t p, const void* k, void* xx, void* stream) {
     NUFFT_TRY(need_plan(p, "nufft_k2xx"));
     NUFFT_TRY(need_ptrs(k, xx, "nufft_k2xx"));
     cudaStream_t s = as_stream(stream);
+    if (p->B > 1) return image_from_spectrum_coils(p, (const float2*)k, (float2*)xx, false, false, s);
     const size_t n = (size_t)p->ninst * p->prodK * p->B;
     NUFFT_CUDA_TRY(cudaMemcpyAsync(p->d_grid, k, sizeof(float2) * n, cudaMemcpyDeviceToDevice, s));
     NUFFT_TRY(fft_exec(p, p->d_grid, +1, s));
@@ -340,6 +341,7 @@ int nufft_adjoint(nufft_plan_t p, const void* y, void* x, void* stream) {
     NUFFT_TRY(need_ptrs(x, y, "nufft_adjoint", p));
     cudaStream_t s = as_stream(stream);
     NUFFT_TRY(launch_y2k(p, (const float2*)y, p->d_grid, s));
+    if (p->B > 1) return image_from_spectrum_coils(p, p->d_grid, (float2*)x, true, false, s);
     NUFFT_TRY(fft_exec(p, p->d_grid, +1, s));
     return launch_crop(p, p->d_grid, (float2*)x, true, false, s);
 }

@@ -214,6 +214,82 @@ __global__ void crop_rows_kernel(ImgGeom g, const float2* __restrict__ grid, flo
   }
 }
 
+// Several coils, coil-major spectra.  The grid of system (instance, coil)
+// = inst * B + b is one contiguous Kd block of `cm`.  Pad: one block per grid
+// row (inst, leading indices) writes that row for every coil (zero outside
+// the Nd corner), reading the coil-fastest image row once through L1.
+template <int DIM>
+__global__ void pad_cm_rows_kernel(ImgGeom g, const float2* __restrict__ xx, float2* __restrict__ cm,
+                                   int apply_sn, int64_t rows) {
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    int64_t inst;
+    int n[3] = {0, 0, 0};
+    row_index<DIM>(r, g.K[0], g.K[1], inst, n[0], n[1]);
+    bool inside = true;
+#pragma unroll
+    for (int d = 0; d < DIM - 1; ++d) inside = inside && (n[d] < g.N[d]);
+    constexpr int last = DIM - 1;
+    const int KL = g.K[last], NL = g.N[last];
+    const int B = g.B;
+    int64_t klocal = 0, xrow = inst;
+#pragma unroll
+    for (int d = 0; d < last; ++d) {
+        klocal = klocal * g.K[d] + n[d];
+        xrow = xrow * g.N[d] + n[d];
+    }
+    const float s_lead = (apply_sn && inside) ? lead_sn<DIM>(g.sn[0], g.sn[1], n[0], n[1]) : 1.f;
+    const float2* src = xx + (size_t)xrow * NL * B;
+    for (int e = threadIdx.x; e < KL * B; e += blockDim.x) {
+        const int b = e / KL, k = e - b * KL;
+        float2 v = make_float2(0.f, 0.f);
+        if (inside && k < NL) {
+            v = __ldg(src + (size_t)k * B + b);
+            if (apply_sn) {
+                const float sc = s_lead * __ldg(g.sn[last] + k);
+                v.x *= sc;
+                v.y *= sc;
+            }
+        }
+        cm[((size_t)inst * B + b) * g.prodK + (size_t)klocal * KL + k] = v;
+    }
+  }
+}
+
+// Crop from coil-major spectra: one block per image row writes that row of
+// every coil into the coil-fastest image (x 1/prod(Kd), x sn if apply_sn,
+// / sn if divide_sn).
+template <int DIM>
+__global__ void crop_cm_rows_kernel(ImgGeom g, const float2* __restrict__ cm, float2* __restrict__ xx,
+                                    int apply_sn, int divide_sn, float norm, int64_t rows) {
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    int64_t inst;
+    int n[3] = {0, 0, 0};
+    row_index<DIM>(r, g.N[0], g.N[1], inst, n[0], n[1]);
+    constexpr int last = DIM - 1;
+    const int KL = g.K[last], NL = g.N[last];
+    const int B = g.B;
+    const float s_lead = lead_sn<DIM>(g.sn[0], g.sn[1], n[0], n[1]);
+    int64_t klocal = 0;
+#pragma unroll
+    for (int d = 0; d < last; ++d) klocal = klocal * g.K[d] + n[d];
+    float2* dst = xx + (size_t)r * NL * B;
+    for (int e = threadIdx.x; e < NL * B; e += blockDim.x) {
+        const int b = e / NL, k = e - b * NL;
+        float2 v = __ldg(cm + ((size_t)inst * B + b) * g.prodK + (size_t)klocal * KL + k);
+        float sc = norm;
+        const float snv = s_lead * __ldg(g.sn[last] + k);
+        if (apply_sn) sc *= snv;
+        v.x *= sc;
+        v.y *= sc;
+        if (divide_sn) {
+            v.x /= snv;
+            v.y /= snv;
+        }
+        dst[(size_t)k * B + b] = v;
+    }
+  }
+}
+
 // SENSE coil expansion fused into x2xx + zero-pad (forward_one2many of the
 // deprecated reference class, linalg/nufft_cpu.py:177-189): the single-coil
 // image x (Nd) times each coil map (Nd, B) times sn, written into the
@@ -334,6 +410,57 @@ int launch_pad(const nufft_plan_s* p, const float2* xx, float2* grid, bool apply
     return check_launch("pad_rows_kernel");
 }
 
+static int coil_transpose(const nufft_plan_s* p, const float2* in, float2* out, bool to_major,
+                          cudaStream_t s);
+
+// Transforms of the coil-major spectra: per system the pruned slab + x-axis
+// FFTs (3D plans with at most 16 systems), else one batched plan.
+static int fft_cm_exec(nufft_plan_s* p, int direction, cudaStream_t s) {
+    const int dir = (direction < 0) ? CUFFT_FORWARD : CUFFT_INVERSE;
+    cufftComplex* cm = reinterpret_cast<cufftComplex*>(p->d_cm);
+    if (p->fft_cm_pruned) {
+        NUFFT_CUFFT_TRY(cufftSetStream(p->fft_slab, s));
+        NUFFT_CUFFT_TRY(cufftSetStream(p->fft_x, s));
+        const int S = p->ninst * p->B;
+        for (int i = 0; i < S; ++i) {
+            cufftComplex* gi = cm + (size_t)i * p->prodK;
+            if (dir == CUFFT_FORWARD) {
+                NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_slab, gi, gi, dir));
+                NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_x, gi, gi, dir));
+            } else {
+                NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_x, gi, gi, dir));
+                NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_slab, gi, gi, dir));
+            }
+        }
+        return NUFFT_OK;
+    }
+    NUFFT_CUFFT_TRY(cufftSetStream(p->fft, s));
+    NUFFT_CUFFT_TRY(cufftExecC2C(p->fft, cm, cm, dir));
+    return NUFFT_OK;
+}
+
+// Several coils: spectrum k (coil-fastest) -> image xx (coil-fastest):
+// transpose to coil-major, inverse FFTs there, crop straight from the
+// coil-major spectra (x sn when apply_sn, / sn when divide_sn).  k is read
+// only.
+int image_from_spectrum_coils(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn,
+                              bool divide_sn, cudaStream_t s) {
+    NUFFT_TRY(coil_transpose(p, k, p->d_cm, true, s));
+    NUFFT_TRY(fft_cm_exec(p, +1, s));
+    ImgGeom g = img_geom(p);
+    const float norm = (float)(1.0 / (double)p->prodK);
+    const int64_t rows = rows_of(g, g.N, p->ninst);
+    const unsigned nb = row_blocks(p, rows);
+    const int nt = row_threads(g.N[g.ndim - 1] * g.B);
+    const int as = apply_sn ? 1 : 0, ds = divide_sn ? 1 : 0;
+    switch (p->ndim) {
+        case 1: crop_cm_rows_kernel<1><<<nb, nt, 0, s>>>(g, p->d_cm, xx, as, ds, norm, rows); break;
+        case 2: crop_cm_rows_kernel<2><<<nb, nt, 0, s>>>(g, p->d_cm, xx, as, ds, norm, rows); break;
+        default: crop_cm_rows_kernel<3><<<nb, nt, 0, s>>>(g, p->d_cm, xx, as, ds, norm, rows); break;
+    }
+    return check_launch("crop_cm_rows_kernel");
+}
+
 // Image (Nd, caller's layout) -> oversampled spectrum k: zero-pad (x sn when
 // apply_sn) and forward FFT.  For one coil and one instance the pad only
 // writes the Nd corner of the plan's padded input buffer (its zeros are
@@ -343,6 +470,22 @@ int launch_pad(const nufft_plan_s* p, const float2* xx, float2* grid, bool apply
 // every call.
 int forward_from_image(nufft_plan_s* p, const float2* xx, bool apply_sn, float2* k,
                        cudaStream_t s) {
+    if (p->B > 1) {
+        // coil-major: pad every coil's grid, transform there, transpose to k
+        ImgGeom g = img_geom(p);
+        const int64_t rows = rows_of(g, g.K, p->ninst);
+        const unsigned nb = row_blocks(p, rows);
+        const int nt = row_threads(g.K[g.ndim - 1] * g.B);
+        const int as = apply_sn ? 1 : 0;
+        switch (p->ndim) {
+            case 1: pad_cm_rows_kernel<1><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, rows); break;
+            case 2: pad_cm_rows_kernel<2><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, rows); break;
+            default: pad_cm_rows_kernel<3><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, rows); break;
+        }
+        NUFFT_TRY(check_launch("pad_cm_rows_kernel"));
+        NUFFT_TRY(fft_cm_exec(p, -1, s));
+        return coil_transpose(p, p->d_cm, k, false, s);
+    }
     if (!(p->fft_pruned && p->d_padin)) {
         NUFFT_TRY(launch_pad(p, xx, k, apply_sn, -1, s));
         return fft_exec(p, k, -1, s);
@@ -501,6 +644,13 @@ int fft_init(nufft_plan_s* p) {
         NUFFT_TRY(make_plan(&p->fft_slab, p->ndim - 1, n + 1, 1, slab, p->Nd[0], &work));
         NUFFT_TRY(make_plan(&p->fft_x, 1, n, slab, 1, slab, &work));
         p->fft_pruned = true;
+    } else if (B > 1 && p->ndim == 3 && p->Nd[0] < p->Kd[0] && p->ninst * B <= 16) {
+        // coil-major spectra of a few 3D systems: the same pruned pair of
+        // plans, run once per system
+        const int slab = (int)(p->prodK / p->Kd[0]);
+        NUFFT_TRY(make_plan(&p->fft_slab, p->ndim - 1, n + 1, 1, slab, p->Nd[0], &work));
+        NUFFT_TRY(make_plan(&p->fft_x, 1, n, slab, 1, slab, &work));
+        p->fft_cm_pruned = true;
     }
     if (work > 0) {
         NUFFT_CUDA_TRY(cudaMalloc(&p->d_fftwork, work));
@@ -516,7 +666,7 @@ int fft_init(nufft_plan_s* p) {
         p->dev_bytes += sizeof(float2) * (nin + p->prodK);
     }
     NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft, p->d_fftwork));
-    if (p->fft_pruned) {
+    if (p->fft_pruned || p->fft_cm_pruned) {
         NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_slab, p->d_fftwork));
         NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_x, p->d_fftwork));
     }
@@ -525,11 +675,11 @@ int fft_init(nufft_plan_s* p) {
 
 void fft_destroy(nufft_plan_s* p) {
     if (p->fft_ok) cufftDestroy(p->fft);
-    if (p->fft_pruned) {
+    if (p->fft_pruned || p->fft_cm_pruned) {
         cufftDestroy(p->fft_slab);
         cufftDestroy(p->fft_x);
     }
-    p->fft_ok = p->fft_pruned = false;
+    p->fft_ok = p->fft_pruned = p->fft_cm_pruned = false;
     cudaFree(p->d_fftwork);
     p->d_fftwork = nullptr;
     cudaFree(p->d_padin);

@@ -146,6 +146,7 @@ struct nufft_plan_s {
     cufftHandle fft_slab = 0;         // (y[,z]) FFTs on the first Nd[0] slabs
     cufftHandle fft_x = 0;            // x-axis FFTs over all slabs
     bool fft_ok = false, fft_pruned = false;
+    bool fft_cm_pruned = false;       // B > 1: per-system pruned plans on the coil-major copy
     void* d_fftwork = nullptr;        // shared cuFFT work area
     float2* d_padin = nullptr;        // pruned forward: zero-padded input, first Nd[0] slabs
     float2* d_slabout = nullptr;      // pruned forward: slab-FFT output, other slabs zero
@@ -210,6 +211,8 @@ int launch_crop(const nufft_plan_s* p, const float2* grid, float2* xx, bool appl
 int fft_exec(nufft_plan_s* p, float2* grid, int direction, cudaStream_t s);
 int forward_from_image(nufft_plan_s* p, const float2* xx, bool apply_sn, float2* k,
                        cudaStream_t s);
+int image_from_spectrum_coils(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn,
+                              bool divide_sn, cudaStream_t s);
 int launch_pad_sense(const nufft_plan_s* p, const float2* x, float2* grid, cudaStream_t s);
 int launch_crop_sense(const nufft_plan_s* p, const float2* grid, float2* x, cudaStream_t s);
 int fft_init(nufft_plan_s* p);
