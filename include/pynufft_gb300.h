@@ -117,6 +117,14 @@ int nufft_plan_set_bins(nufft_plan_t plan, const int* bin_shape, int max_sub_poi
                                (no shared tile; not in deterministic mode)    */
 int nufft_plan_set_methods(nufft_plan_t plan, int k2y_method, int y2k_method);
 
+/* Device address of page-locked host memory that is mapped into the device
+ * address space (cudaHostAlloc / pinned tensors on unified-addressing
+ * systems), for passing a host image straight to nufft_forward (read) or
+ * nufft_adjoint (written) instead of copying it: the image kernels then access
+ * host memory over the host link.  NUFFT_EINVAL if `host` is not such memory.
+ * No counterpart in the reference. */
+int nufft_mapped_pointer(const void* host, void** dev_out);
+
 /* Synchronise `stream` and report whether any kernel of this plan gave up a
  * bounded wait for its asynchronous (bulk-copy) loads since the last check:
  * NUFFT_ETIMEOUT if so (that launch's output is incomplete; the flag is

@@ -272,6 +272,26 @@ int nufft_plan_info(nufft_plan_t p, int64_t* M_total, int64_t* n_sub, int64_t* d
     return NUFFT_OK;
 }
 
+int nufft_mapped_pointer(const void* host, void** dev_out) {
+    if (!host || !dev_out) {
+        set_error("nufft_mapped_pointer: NULL argument");
+        return NUFFT_EINVAL;
+    }
+    cudaPointerAttributes a{};
+    cudaError_t e = cudaPointerGetAttributes(&a, host);
+    if (e != cudaSuccess) {
+        cudaGetLastError();   // clear the sticky-free error of an unknown pointer
+        set_error(std::string("nufft_mapped_pointer: ") + cudaGetErrorString(e));
+        return NUFFT_EINVAL;
+    }
+    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) {
+        set_error("nufft_mapped_pointer: not page-locked host memory mapped into the device");
+        return NUFFT_EINVAL;
+    }
+    *dev_out = a.devicePointer;
+    return NUFFT_OK;
+}
+
 int nufft_plan_check(nufft_plan_t p, void* stream) {
     NUFFT_TRY(need_plan(p, "nufft_plan_check"));
     int h = 0;

@@ -313,13 +313,38 @@ class NUFFT:
         torch = _torch()
         return torch.empty(self._shape(kind), dtype=torch.complex64, device=self.device)
 
+    def _mapped(self, t):
+        """Device address of a pinned CPU tensor mapped into the device, or None."""
+        dev = c_void_p()
+        if self._lib.nufft_mapped_pointer(c_void_p(t.data_ptr()), ctypes.byref(dev)) != _lib.NUFFT_OK:
+            return None
+        return dev
+
     def _call(self, fn, a, kin, kout, name):
         torch = _torch()
-        d, how = self._in(a, kin)
-        out = self._empty(kout)
+        # pinned CPU images are read (kin 'x') and written (kout 'x') by the
+        # streaming image kernels in place over the host link, without a copy
+        host_in = (kin == 'x' and isinstance(a, torch.Tensor) and not a.is_cuda
+                   and a.is_pinned() and a.dtype == torch.complex64 and a.is_contiguous()
+                   and tuple(a.shape) == self._shape('x'))
+        inptr = self._mapped(a) if host_in else None
+        if inptr is not None:
+            how = ('cpu', True)
+        else:
+            d, how = self._in(a, kin)
+            inptr = c_void_p(d.data_ptr())
+        out, outptr = None, None
+        if kout == 'x' and how == ('cpu', True):
+            out = torch.empty(self._shape('x'), dtype=torch.complex64, pin_memory=True)
+            outptr = self._mapped(out)
+        if outptr is None:
+            out = self._empty(kout)
+            outptr = c_void_p(out.data_ptr())
         with torch.cuda.device(self.device):
-            _lib.check(fn(self._plan, c_void_p(d.data_ptr()), c_void_p(out.data_ptr()),
-                          self._stream()), name)
+            _lib.check(fn(self._plan, inptr, outptr, self._stream()), name)
+            if not out.is_cuda:
+                torch.cuda.current_stream(self.device).synchronize()
+                return out
         return self._out(out, how)
 
     # ------------------------------------------------------------ operators

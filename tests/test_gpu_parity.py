@@ -377,3 +377,28 @@ def test_cg_on_many_instances_and_coils_matches_oracle(NUFFT):
             else:
                 assert rel_l2(x[i][..., b], xo[..., b]) < 1e-4
         off += Ms[i]
+
+
+@pytest.mark.parametrize('B', [None, 4])
+def test_pinned_host_images_match_device_tensors(NUFFT, B):
+    """Pinned CPU tensors: the image kernels read and write them in place
+    through their device mapping (no copies); results equal the device-tensor
+    path and the returned tensors are pinned CPU tensors."""
+    import torch
+    rng = np.random.default_rng(41)
+    Nd, Kd, Jd = (24, 20, 16), (48, 40, 32), (6, 6, 6)
+    M = 3000
+    om = rng.uniform(-np.pi, np.pi, (M, 3))
+    A = NUFFT(0)
+    A.plan(om, Nd, Kd, Jd, batch=B)
+    tail = () if B is None else (B,)
+    x = torch.from_numpy(cplx(rng, Nd + tail)).pin_memory()
+    y = torch.from_numpy(cplx(rng, (M,) + tail)).pin_memory()
+    k = torch.from_numpy(cplx(rng, Kd + tail)).pin_memory()
+    xd, yd, kd = x.cuda(), y.cuda(), k.cuda()
+    for name, arg, argd in [('forward', x, xd), ('adjoint', y, yd), ('selfadjoint', x, xd),
+                            ('x2xx', x, xd), ('xx2x', x, xd), ('xx2k', x, xd), ('k2xx', k, kd)]:
+        got = getattr(A, name)(arg)
+        ref = getattr(A, name)(argd).cpu()
+        assert not got.is_cuda and got.is_pinned(), name
+        assert rel_l2(got.numpy(), ref.numpy()) < 1e-6, name
