@@ -125,6 +125,12 @@ int nufft_plan_set_methods(nufft_plan_t plan, int k2y_method, int y2k_method);
  * No counterpart in the reference. */
 int nufft_mapped_pointer(const void* host, void** dev_out);
 
+/* Self-test of the bounded wait the bulk-copy kernels use: one block waits
+ * `polls` polls (1 .. 2^22) on an mbarrier whose bytes never arrive and
+ * *timed_out receives 1 if the wait ran out (the expected answer).  Faults and
+ * hangs nothing; synchronises the device.  No counterpart in the reference. */
+int nufft_selftest_bounded_wait(int polls, int* timed_out);
+
 /* Synchronise `stream` and report whether any kernel of this plan gave up a
  * bounded wait for its asynchronous (bulk-copy) loads since the last check:
  * NUFFT_ETIMEOUT if so (that launch's output is incomplete; the flag is

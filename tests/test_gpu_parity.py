@@ -402,3 +402,20 @@ def test_pinned_host_images_match_device_tensors(NUFFT, B):
         ref = getattr(A, name)(argd).cpu()
         assert not got.is_cuda and got.is_pinned(), name
         assert rel_l2(got.numpy(), ref.numpy()) < 1e-6, name
+
+
+def test_bounded_wait_runs_out_and_the_context_stays_usable(NUFFT):
+    """The bounded mbarrier wait of the bulk-copy kernels ends when its bytes
+    never arrive (a self-test kernel arms 16 bytes that no copy delivers),
+    reports it, and the GPU keeps working; a plan's own flag stays clear."""
+    import ctypes
+    from pynufft_gb300 import _lib
+    L = _lib.load()
+    t = ctypes.c_int(0)
+    _lib.check(L.nufft_selftest_bounded_wait(1000, ctypes.byref(t)), 'selftest')
+    assert t.value == 1
+    g = load_golden('plan_2d')
+    A = NUFFT(0)
+    A.plan(g['om'], _tup(g['Nd']), _tup(g['Kd']), _tup(g['Jd']))
+    assert rel_l2(A.forward(g['x']), g['forward']) < TOL
+    A.check()
