@@ -686,7 +686,7 @@ __global__ void __launch_bounds__(256) k2y_spoint_kernel(Geom g, const float2* _
 // of once per point that covers it.  EX: every axis has exactly JM taps.
 // ---------------------------------------------------------------------------
 template <int DIM, int JM, int G, bool EX>
-__global__ void __launch_bounds__(256) k2y_ctile_kernel(Geom g, const float2* __restrict__ grid,
+__global__ void __launch_bounds__(512) k2y_ctile_kernel(Geom g, const float2* __restrict__ grid,
                                                         float2* __restrict__ y) {
     static_assert(DIM > 1, "tiles of rows");
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1183,7 +1183,7 @@ __global__ void __launch_bounds__(256) y2k_spoint_kernel(Geom g, const float2* _
 // y2k, coil-teams (B >= 8): tile layout cell-major, coil fastest
 // ---------------------------------------------------------------------------
 template <int DIM, int JM, int G, bool DET, bool EX>
-__global__ void __launch_bounds__(256) y2k_coil_kernel(Geom g, const float2* __restrict__ y,
+__global__ void __launch_bounds__(512) y2k_coil_kernel(Geom g, const float2* __restrict__ y,
                                                        float2* __restrict__ grid,
                                                        unsigned long long* __restrict__ igrid,
                                                        int bc, const double* __restrict__ dscal) {

@@ -81,7 +81,7 @@ static void k2y_launch(const Geom& g, const float2* grid, float2* y, cudaStream_
                     exact ? k2y_ctile_kernel<DIM, JM, G, true> : k2y_ctile_kernel<DIM, JM, G, false>;
                 if (smem > 48 * 1024)
                     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                kern<<<(unsigned)g.nsub, threads, smem, s>>>(g, grid, y);
+                kern<<<(unsigned)g.nsub, 512, smem, s>>>(g, grid, y);
                 return;
             }
         }
@@ -180,6 +180,7 @@ static int y2k_launch(const Geom& g, const float2* y, float2* grid, unsigned lon
         bool exact = true;
         for (int d = 0; d < DIM; ++d) exact = exact && (g.J[d] == JM);
         kern = exact ? y2k_coil_kernel<DIM, JM, G, DET, true> : y2k_coil_kernel<DIM, JM, G, DET, false>;
+        threads = 512;
     }
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
