@@ -47,6 +47,9 @@ CONFIGS = {
                Nd=(256, 256), Kd=(512, 512), Jd=(6, 6), batch=8),
     'c5': dict(name='3D kooshball 15625x512 (M=8,000,000), Nd 192^3, Kd 384^3, Jd 6^3, 8 coils, fwd+adj pair',
                Nd=(192, 192, 192), Kd=(384, 384, 384), Jd=(6, 6, 6), batch=8),
+    'c3i': dict(name='64 independent 2D uniform instances, M ~ U{20000..200000} each, Nd 320^2, Kd 640^2, '
+                     'Jd 6^2, one fwd+adj of every instance per step (a pair = one instance)',
+                Nd=(320, 320), Kd=(640, 640), Jd=(6, 6), batch=None, ninst=64),
 }
 
 
@@ -65,6 +68,9 @@ def workload(cfg: str):
     elif cfg == 'c4':
         om = T.spiral_2d(32, 2048, seed=6)
         x = T.random_image(c['Nd'] + (8,), seed=0)
+    elif cfg == 'c3i':
+        om = T.uneven_instances(c['ninst'], seed=5)
+        x = T.random_image((c['ninst'],) + c['Nd'], seed=0)
     else:
         om = T.kooshball_3d(15625, 512)
         x = T.random_image(c['Nd'] + (8,), seed=0)
@@ -78,7 +84,7 @@ def alg_bytes(c, M):
     d = len(c['Nd'])
     C = c['batch'] or 1
     meta = 8 * sum(c['Jd']) + 4 * d
-    return M * meta + C * (8 * M + 8 * int(np.prod(c['Kd'])))
+    return M * meta + C * (8 * M + 8 * int(np.prod(c['Kd'])) * c.get('ninst', 1))
 
 
 def peaks():
@@ -187,6 +193,10 @@ def run_reference(args, cfg, rank):
     if rank != 0:
         return
     c, om, x = workload(cfg)
+    if c.get('ninst', 1) > 1:
+        print(json.dumps({'impl': 'reference', 'unavailable': 'the CPU reference arm times '
+                          'single-instance configurations only'}), flush=True)
+        return
     threads = os.cpu_count() or 1
     v, sample, t_pair = cpu_baseline(cfg, c, om, x, threads=threads, steps=args.steps,
                                      warmup=args.warmup)
@@ -232,13 +242,20 @@ def main():
     c, om, x = workload(args.config)
     dev = torch.device('cuda', local)
     A = NUFFT(dev)
-    A.plan(om, c['Nd'], c['Kd'], c['Jd'], batch=c['batch'])
+    ninst = c.get('ninst', 1)
+
+    def make_plan():
+        if ninst > 1:
+            A.plan_many(om, c['Nd'], c['Kd'], c['Jd'], batch=c['batch'])
+        else:
+            A.plan(om, c['Nd'], c['Kd'], c['Jd'], batch=c['batch'])
+    make_plan()
     torch.cuda.synchronize()
     t0 = time.perf_counter()       # second plan: host om, tables rebuilt, no first-use costs
-    A.plan(om, c['Nd'], c['Kd'], c['Jd'], batch=c['batch'])
+    make_plan()
     torch.cuda.synchronize()
     plan_ms = (time.perf_counter() - t0) * 1e3
-    M = om.shape[0]
+    M = sum(o.shape[0] for o in om) if ninst > 1 else om.shape[0]
     xd = torch.from_numpy(x).to(dev)
     yd = torch.empty(A._shape('y'), dtype=torch.complex64, device=dev)
     xo = torch.empty_like(xd)
@@ -252,7 +269,7 @@ def main():
         lib.nufft_adjoint(A._plan, c_void_p(yd.data_ptr()), c_void_p(xo.data_ptr()), sp)
 
     # working set of one step: per-point tables + samples + grid + image
-    ws_bytes = M * (8 * sum(c['Jd']) + 4 * len(c['Nd'])) + 8 * (M + np.prod(c['Kd']) + np.prod(c['Nd'])) * (c['batch'] or 1)
+    ws_bytes = M * (8 * sum(c['Jd']) + 4 * len(c['Nd'])) + 8 * (M + ninst * (np.prod(c['Kd']) + np.prod(c['Nd']))) * (c['batch'] or 1)
     flush = ws_bytes < L2_BYTES
     scratch = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device=dev) if flush else None
 
@@ -293,8 +310,10 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     ms_per_step = ms / args.steps
-    value = world * args.steps / (ms / 1e3)
-    launches_per_step = 4          # pad, k2y, y2k, crop (cuFFT kernels are the library's)
+    value = world * ninst * args.steps / (ms / 1e3)   # many-instance configs count instance pairs
+    # own kernels per step (cuFFT kernels are the library's): pad, k2y, y2k,
+    # crop; several coils add the two coil transposes
+    launches_per_step = 4 if (c['batch'] or 1) == 1 else 6
 
     # dominant kernel alone: k2y and y2k, CUDA events on the launching stream
     def time_call(fn, reps=20):
@@ -344,13 +363,15 @@ def main():
         xs = torch.empty_like(xd)
         it = c_int(0)
 
+        cg_iters = 15 if ninst > 1 else 20    # c3 many-instance: 15 per instance; c2: 20
+
         def solve():
-            lib.nufft_solve_cg(A._plan, c_void_p(yn.data_ptr()), c_void_p(xs.data_ptr()), 20,
+            lib.nufft_solve_cg(A._plan, c_void_p(yn.data_ptr()), c_void_p(xs.data_ptr()), cg_iters,
                                1e-5, 0.0, None, sp)
         t_cg = time_call(solve, reps=5)
-        lib.nufft_solve_cg(A._plan, c_void_p(yn.data_ptr()), c_void_p(xs.data_ptr()), 20,
+        lib.nufft_solve_cg(A._plan, c_void_p(yn.data_ptr()), c_void_p(xs.data_ptr()), cg_iters,
                            1e-5, 0.0, byref(it), sp)
-        cg = {'maxiter': 20, 'iters': it.value, 'ms': t_cg}
+        cg = {'maxiter': cg_iters, 'iters': it.value, 'ms': t_cg, 'systems': ninst}
 
     # end to end through the public API, pinned host buffers, copies included
     xh = torch.from_numpy(x).pin_memory()
@@ -364,7 +385,7 @@ def main():
         yh = A.forward(xh)
         xr = A.adjoint(yh)
     torch.cuda.synchronize()
-    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    t_e2e = (time.perf_counter() - t0) / e2e_steps / ninst
     if dist:
         t = torch.tensor([t_e2e], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -373,7 +394,7 @@ def main():
     d2h = (yh.numel() + xr.numel()) * 8
 
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and not args.no_cpu and ninst == 1:
         v, sample, _ = cpu_baseline(args.config, c, om, x, threads=1)
         cpu = {'value': v, 'unit': 'pairs/s', 'cores': 1, 'kind': 'port', 'sample': sample}
 
@@ -388,7 +409,7 @@ def main():
                                % (FLUSH_BYTES >> 20, ws_bytes / 1e6)) if flush else
                               'inputs larger than L2 (per-point tables %.0f MB + grid %.0f MB)' % (
                                   M * (8 * sum(c['Jd']) + 4 * len(c['Nd'])) / 1e6,
-                                  8 * np.prod(c['Kd']) * (c['batch'] or 1) / 1e6))},
+                                  8 * np.prod(c['Kd']) * (c['batch'] or 1) * ninst / 1e6))},
             'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': ach, 'peak': peak,
                          'unit': 'GB/s', 'frac': ach / peak, 'peak_kind': peak_kind,
                          'traffic': traffic, 'alg_bytes': nbytes, 'ms': t_dom},
