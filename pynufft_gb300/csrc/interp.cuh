@@ -8,25 +8,26 @@
 // coef_d holds conj(u) exactly as the reference's CSR values
 // (helper.min_max returns u.T.conj(), src/_helper/helper.py:606-618).
 //
-// Two lane mappings, chosen by the coil count B:
-//  * z-teams (B < 8): a team of J_z lanes (J of the innermost axis) shares one
-//    point, lane k owning footprint offset k along the innermost axis.  A
-//    team's grid accesses are J_z consecutive cells, so a warp touches ~2
-//    sectors per team instead of one scattered sector per lane; the sum over
-//    k is a shuffle reduction inside the team.  Coils loop inside the lane.
-//  * coil-teams (B >= 8): G = 8 or 32 lanes share one point and split the
-//    coils, so consecutive lanes touch consecutive coils of one cell.
-// Both factorise the footprint sum axis by axis (outer axis rolled, re-read
-// through L1; middle axis in registers; inner axis across lanes or unrolled).
+// Lane mappings (the defaults; `nufft_plan_set_methods` and the autotuner
+// may choose the others):
+//  * paired threads (one coil, 2D/3D): a block per bin sub-problem stages the
+//    bin's footprint tile in shared memory (bulk copies for k2y, a fixed-
+//    point accumulator for y2k); two threads per point split the outer axis.
+//  * coil teams (B >= 8): G = 8 or 32 lanes share one point and split the
+//    coils, so consecutive lanes touch consecutive coils of one cell; k2y
+//    gathers from a shared tile of all coils.
+//  * one thread per point, z-teams (J lanes per point along the innermost
+//    axis), global atomics: the remaining cases and autotuner candidates.
+// All factorise the footprint sum axis by axis (outer axis rolled, middle
+// axis in registers, inner axis unrolled or across lanes).
 //
 // Gridding accumulates in shared memory with native integer atomics: this
 // GPU has no native shared-memory float add (a float atomicAdd there is a
 // compare-and-swap loop).  The fast mode converts each float contribution to
-// 32-bit fixed point with a power-of-two scale chosen per sub-problem from a
-// bound on any cell's sum (sum over the sub-problem's points of
-// W_p (|re y| + |im y|), W_p = prod_d max_j |coef|), so no cell can overflow
-// and the rounding unit stays below float32 resolution for sub-problems of a
-// few hundred points; the tile is converted back to float and added to the
+// 32-bit fixed point with a scale chosen per sub-problem from a bound on any
+// cell's sum (sum over the sub-problem's points of W_p (|re y| + |im y|),
+// W_p = prod_d max_j |coef|), so no cell can overflow and the rounding unit
+// stays near float32 resolution for sub-problems of a few hundred points; the tile is converted back to float and added to the
 // grid with vector atomics.  The deterministic mode uses 64-bit fixed point
 // with one global scale and flushes integers, so the whole sum is exact and
 // order-independent.
