@@ -853,6 +853,18 @@ __device__ __forceinline__ void flush_tile(const Geom& g, const int (&o)[3], int
                                              __int2float_rn((int)vy) * inv));
         }
     };
+    // a tile that does not wrap around the periodic grid addresses its cells
+    // with multiply-adds instead of wrapping each coordinate
+    bool interior = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) interior = interior && (o[d] + g.T[d] <= g.K[d]);
+    auto gcell = [&](const TileWalk<DIM>& w) -> size_t {
+        if (!interior) return w.cell(g, o);
+        size_t gc = (size_t)(o[0] + w.t[0]);
+#pragma unroll
+        for (int d = 1; d < DIM; ++d) gc = gc * g.K[d] + (size_t)(o[d] + w.t[d]);
+        return gc;
+    };
     if constexpr (CELL_MAJOR) {
         // threads split as (cell, coil), coil fastest (bcur <= blockDim): a
         // warp reads consecutive words of the tile and adds to consecutive
@@ -864,14 +876,14 @@ __device__ __forceinline__ void flush_tile(const Geom& g, const int (&o)[3], int
         TileWalk<DIM> w;
         w.init(g.T, c0, cpb);
         for (int c = c0; c < ncell; c += cpb, w.next())
-            put(c * bcur + b, (ibase + w.cell(g, o)) * B + b0 + b, inv);
+            put(c * bcur + b, (ibase + gcell(w)) * B + b0 + b, inv);
     } else {
         for (int b = 0; b < bcur; ++b) {
             const float inv = DET ? 1.f : 1.f / scale[b];
             TileWalk<DIM> w;
             w.init(g.T, threadIdx.x, blockDim.x);
             for (int c = threadIdx.x; c < ncell; c += blockDim.x, w.next())
-                put(b * ncell + c, (ibase + w.cell(g, o)) * B + b0 + b, inv);
+                put(b * ncell + c, (ibase + gcell(w)) * B + b0 + b, inv);
         }
     }
 }
@@ -1169,14 +1181,33 @@ __global__ void __launch_bounds__(256) y2k_spoint_kernel(Geom g, const float2* _
     for (int d = 0; d < DIM; ++d) ncell *= g.T[d];
     const float inv = 1.f / sc;
     const size_t ibase = (size_t)sp.w * g.prodK;
+    // a tile that does not wrap around the periodic grid (and a grid with
+    // fewer than 2^31 cells) addresses its cells with 32-bit multiply-adds
+    bool interior = g.prodK < ((int64_t)1 << 31);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) interior = interior && (o[d] + g.T[d] <= g.K[d]);
     TileWalk<DIM> w;
     w.init(g.T, threadIdx.x, blockDim.x);
-    for (int c = threadIdx.x; c < ncell; c += blockDim.x, w.next()) {
-        const int a = tile_addr<DIM>(w.t, ts);
-        const unsigned vx = re[a], vy = im[a];
-        if (vx == 0u && vy == 0u) continue;
-        atomicAdd(grid + ibase + w.cell(g, o),
-                  make_float2(__int2float_rn((int)vx) * inv, __int2float_rn((int)vy) * inv));
+    if (interior) {
+        float2* gb = grid + ibase;
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x, w.next()) {
+            const int a = tile_addr<DIM>(w.t, ts);
+            const unsigned vx = re[a], vy = im[a];
+            if (vx == 0u && vy == 0u) continue;
+            int gc = o[0] + w.t[0];
+#pragma unroll
+            for (int d = 1; d < DIM; ++d) gc = gc * g.K[d] + o[d] + w.t[d];
+            atomicAdd(gb + gc,
+                      make_float2(__int2float_rn((int)vx) * inv, __int2float_rn((int)vy) * inv));
+        }
+    } else {
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x, w.next()) {
+            const int a = tile_addr<DIM>(w.t, ts);
+            const unsigned vx = re[a], vy = im[a];
+            if (vx == 0u && vy == 0u) continue;
+            atomicAdd(grid + ibase + w.cell(g, o),
+                      make_float2(__int2float_rn((int)vx) * inv, __int2float_rn((int)vy) * inv));
+        }
     }
 }
 
