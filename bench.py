@@ -12,7 +12,9 @@ between steps.
 Prints ONE JSON line (rank 0).  `value` times steps with inputs resident on
 the device (CUDA events on the launching stream); `e2e` times the public API
 (`NUFFT.forward`/`adjoint` on pinned host tensors, copies included);
-`roofline` times the dominant kernel alone with CUDA events;
+`roofline` uses the dominant kernel's own average duration, from CUDA events
+that the library records around each of its launches on the launching stream
+during the timed steps;
 `cpu_baseline` times the CPU oracle (a restatement of the reference numpy
 path) on a bounded sample.  With --gpus N > 1 (torchrun) every rank runs an
 independent replica of the workload (no collective on the data path) and
@@ -276,6 +278,10 @@ def main():
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
+    # the dominant kernels' own durations, from CUDA events the library
+    # records around each k2y / y2k launch on the launching stream during the
+    # timed steps
+    lib.nufft_plan_kernel_timing(A._plan, 1)
     clocks = ClockSampler(local)
     clocks.start()
     if dist:
@@ -305,6 +311,12 @@ def main():
     if dist:
         dist.barrier()
     clk = clocks.stop()
+    from ctypes import byref, c_double, c_int
+    k_ms, y_ms, k_n, y_n = c_double(), c_double(), c_int(), c_int()
+    lib.nufft_plan_kernel_times(A._plan, byref(k_ms), byref(k_n), byref(y_ms), byref(y_n))
+    lib.nufft_plan_kernel_timing(A._plan, 0)
+    t_k2y = k_ms.value / max(k_n.value, 1)
+    t_y2k = y_ms.value / max(y_n.value, 1)
     if dist:
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -339,12 +351,6 @@ def main():
         torch.cuda.synchronize()
         return a.elapsed_time(b) / reps
 
-    grid = torch.empty(A._shape('k'), dtype=torch.complex64, device=dev)
-    lib.nufft_xx2k(A._plan, c_void_p(xd.data_ptr()), c_void_p(grid.data_ptr()), sp)
-    t_k2y = time_call(lambda: lib.nufft_k2y(A._plan, c_void_p(grid.data_ptr()),
-                                            c_void_p(yd.data_ptr()), sp))
-    t_y2k = time_call(lambda: lib.nufft_y2k(A._plan, c_void_p(yd.data_ptr()),
-                                            c_void_p(grid.data_ptr()), sp))
     nbytes = alg_bytes(c, M)
     peak, peak_kind = peaks()
     dom = 'y2k' if t_y2k >= t_k2y else 'k2y'
@@ -412,7 +418,8 @@ def main():
                                   8 * np.prod(c['Kd']) * (c['batch'] or 1) * ninst / 1e6))},
             'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': ach, 'peak': peak,
                          'unit': 'GB/s', 'frac': ach / peak, 'peak_kind': peak_kind,
-                         'traffic': traffic, 'alg_bytes': nbytes, 'ms': t_dom},
+                         'traffic': traffic, 'alg_bytes': nbytes, 'ms': t_dom,
+                         'timed_launches': y_n.value if dom == 'y2k' else k_n.value},
             'gridding': {'kernel': 'y2k', 'ms': t_y2k, 'gbs': nbytes / (t_y2k / 1e3) / 1e9,
                          'frac': nbytes / (t_y2k / 1e3) / 1e9 / peak},
             'interp': {'kernel': 'k2y', 'ms': t_k2y, 'gbs': nbytes / (t_k2y / 1e3) / 1e9,

@@ -117,6 +117,17 @@ int nufft_plan_set_bins(nufft_plan_t plan, const int* bin_shape, int max_sub_poi
                                (no shared tile; not in deterministic mode)    */
 int nufft_plan_set_methods(nufft_plan_t plan, int k2y_method, int y2k_method);
 
+/* Optional timing of the interpolation (k2y) and gridding (y2k) kernels:
+ * while enabled, every k2y / y2k kernel launch of this plan is bracketed by a
+ * pair of CUDA events on its own stream (skipped while the stream is being
+ * captured into a graph).  nufft_plan_kernel_times waits for the recorded
+ * events and returns the summed kernel time (ms) and the number of launches
+ * of each, then forgets them.  Enabling or disabling also forgets them.  No
+ * counterpart in the reference. */
+int nufft_plan_kernel_timing(nufft_plan_t plan, int enable);
+int nufft_plan_kernel_times(nufft_plan_t plan, double* k2y_ms, int* k2y_launches,
+                            double* y2k_ms, int* y2k_launches);
+
 /* Device address of page-locked host memory that is mapped into the device
  * address space (cudaHostAlloc / pinned tensors on unified-addressing
  * systems), for passing a host image straight to nufft_forward (read) or

@@ -57,6 +57,9 @@ SIGNATURES = {
     'nufft_plan_check': (c_int, [c_void_p, c_void_p]),
     'nufft_mapped_pointer': (c_int, [c_void_p, POINTER(c_void_p)]),
     'nufft_selftest_bounded_wait': (c_int, [c_int, POINTER(c_int)]),
+    'nufft_plan_kernel_timing': (c_int, [c_void_p, c_int]),
+    'nufft_plan_kernel_times': (c_int, [c_void_p, POINTER(c_double), POINTER(c_int),
+                                        POINTER(c_double), POINTER(c_int)]),
     'nufft_forward_dom': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     'nufft_set_sense': (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
     'nufft_y2k_exact_static': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -191,6 +191,7 @@ int nufft_plan_destroy(nufft_plan_t p) {
     cudaFree(p->d_dscal);
     cudaFree(p->d_maps);
     cudaFree(p->d_kerr);
+    kernel_time_clear(p);
     delete p;
     return NUFFT_OK;
 }
@@ -269,6 +270,34 @@ int nufft_plan_info(nufft_plan_t p, int64_t* M_total, int64_t* n_sub, int64_t* d
         }
         *device_bytes = (int64_t)p->dev_bytes + pts;
     }
+    return NUFFT_OK;
+}
+
+int nufft_plan_kernel_timing(nufft_plan_t p, int enable) {
+    NUFFT_TRY(need_plan(p, "nufft_plan_kernel_timing"));
+    kernel_time_clear(p);
+    p->ktime = enable != 0;
+    return NUFFT_OK;
+}
+
+int nufft_plan_kernel_times(nufft_plan_t p, double* k2y_ms, int* k2y_launches, double* y2k_ms,
+                            int* y2k_launches) {
+    NUFFT_TRY(need_plan(p, "nufft_plan_kernel_times"));
+    double* ms[2] = {k2y_ms, y2k_ms};
+    int* n[2] = {k2y_launches, y2k_launches};
+    for (int w = 0; w < 2; ++w) {
+        double tot = 0.0;
+        const size_t pairs = p->kev[w].size() / 2;
+        for (size_t i = 0; i < pairs; ++i) {
+            NUFFT_CUDA_TRY(cudaEventSynchronize(p->kev[w][2 * i + 1]));
+            float t = 0.f;
+            NUFFT_CUDA_TRY(cudaEventElapsedTime(&t, p->kev[w][2 * i], p->kev[w][2 * i + 1]));
+            tot += t;
+        }
+        if (ms[w]) *ms[w] = tot;
+        if (n[w]) *n[w] = (int)pairs;
+    }
+    kernel_time_clear(p);
     return NUFFT_OK;
 }
 

@@ -30,15 +30,36 @@ static int pick_jm(const nufft_plan_s* p) {
 // ---------------------------------------------------------------------------
 // k2y
 // ---------------------------------------------------------------------------
-int launch_k2y(const nufft_plan_s* p, const float2* grid, float2* y, cudaStream_t s) {
+// Optional kernel timing: an event pair recorded around each k2y / y2k
+// kernel launch on its own stream (not while the stream is being captured).
+void kernel_time_mark(nufft_plan_s* p, int which, cudaStream_t s) {
+    if (!p->ktime) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return;
+    cudaEventRecord(e, s);
+    p->kev[which].push_back(e);
+}
+
+void kernel_time_clear(nufft_plan_s* p) {
+    for (int w = 0; w < 2; ++w) {
+        for (cudaEvent_t e : p->kev[w]) cudaEventDestroy(e);
+        p->kev[w].clear();
+    }
+}
+
+int launch_k2y(nufft_plan_s* p, const float2* grid, float2* y, cudaStream_t s) {
     if (p->M == 0) return NUFFT_OK;
     Geom g = p->geom();
     const int jm = pick_jm(p);
+    kernel_time_mark(p, 0, s);
     switch (p->ndim) {
         case 1: k2y_dim1(jm, g, grid, y, s); break;
         case 2: k2y_dim2(jm, g, grid, y, s); break;
         default: k2y_dim3(jm, g, grid, y, s); break;
     }
+    kernel_time_mark(p, 0, s);
     return check_launch("k2y_kernel");
 }
 
@@ -115,7 +136,10 @@ int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s) {
     if (!(p->flags & NUFFT_FLAG_DETERMINISTIC)) {
         NUFFT_CUDA_TRY(cudaMemsetAsync(grid, 0, sizeof(float2) * ncells, s));
         if (p->M == 0) return NUFFT_OK;
-        return y2k_dim<false>(p, g, y, grid, nullptr, nullptr, s);
+        kernel_time_mark(p, 1, s);
+        const int st = y2k_dim<false>(p, g, y, grid, nullptr, nullptr, s);
+        kernel_time_mark(p, 1, s);
+        return st;
     }
     // deterministic: exact fixed-point accumulation, then one rounding to float
     if (!p->d_igrid) {

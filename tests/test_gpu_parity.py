@@ -447,3 +447,23 @@ def test_odd_grids_and_mixed_J_match_oracle(NUFFT, Nd, Kd, Jd):
     assert rel_l2(A.forward(x), O.forward(x)) < TOL
     assert rel_l2(A.adjoint(y), O.adjoint(y)) < TOL
     A.check()
+
+
+def test_kernel_timing_counts_the_launches(NUFFT):
+    """nufft_plan_kernel_timing brackets every k2y / y2k kernel launch with
+    CUDA events: a forward and an adjoint give one timed launch of each."""
+    import ctypes
+    g = load_golden('plan_3d')
+    A = NUFFT(0)
+    A.plan(g['om'], _tup(g['Nd']), _tup(g['Kd']), _tup(g['Jd']))
+    L, P = A._lib, A._plan
+    L.nufft_plan_kernel_timing(P, 1)
+    A.forward(g['x'])
+    A.adjoint(g['y'])
+    km, ym = ctypes.c_double(), ctypes.c_double()
+    kn, yn = ctypes.c_int(), ctypes.c_int()
+    assert L.nufft_plan_kernel_times(P, ctypes.byref(km), ctypes.byref(kn), ctypes.byref(ym),
+                                     ctypes.byref(yn)) == 0
+    L.nufft_plan_kernel_timing(P, 0)
+    assert kn.value == 1 and yn.value == 1
+    assert km.value > 0 and ym.value > 0
