@@ -191,7 +191,7 @@ int nufft_plan_destroy(nufft_plan_t p) {
     cudaFree(p->d_dscal);
     cudaFree(p->d_maps);
     cudaFree(p->d_kerr);
-    kernel_time_clear(p);
+    kernel_time_destroy(p);
     delete p;
     return NUFFT_OK;
 }
@@ -287,7 +287,7 @@ int nufft_plan_kernel_times(nufft_plan_t p, double* k2y_ms, int* k2y_launches, d
     int* n[2] = {k2y_launches, y2k_launches};
     for (int w = 0; w < 2; ++w) {
         double tot = 0.0;
-        const size_t pairs = p->kev[w].size() / 2;
+        const size_t pairs = p->kused[w] / 2;
         for (size_t i = 0; i < pairs; ++i) {
             NUFFT_CUDA_TRY(cudaEventSynchronize(p->kev[w][2 * i + 1]));
             float t = 0.f;

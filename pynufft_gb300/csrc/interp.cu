@@ -36,16 +36,22 @@ void kernel_time_mark(nufft_plan_s* p, int which, cudaStream_t s) {
     if (!p->ktime) return;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
-    cudaEvent_t e;
-    if (cudaEventCreate(&e) != cudaSuccess) return;
-    cudaEventRecord(e, s);
-    p->kev[which].push_back(e);
+    std::vector<cudaEvent_t>& v = p->kev[which];
+    if (p->kused[which] == v.size()) {   // grow the pool (amortised: events are reused)
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        v.push_back(e);
+    }
+    cudaEventRecord(v[p->kused[which]++], s);
 }
 
-void kernel_time_clear(nufft_plan_s* p) {
+void kernel_time_clear(nufft_plan_s* p) { p->kused[0] = p->kused[1] = 0; }
+
+void kernel_time_destroy(nufft_plan_s* p) {
     for (int w = 0; w < 2; ++w) {
         for (cudaEvent_t e : p->kev[w]) cudaEventDestroy(e);
         p->kev[w].clear();
+        p->kused[w] = 0;
     }
 }
 

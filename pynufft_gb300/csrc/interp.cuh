@@ -1215,7 +1215,7 @@ __global__ void __launch_bounds__(256) y2k_spoint_kernel(Geom g, const float2* _
 // y2k, coil-teams (B >= 8): tile layout cell-major, coil fastest
 // ---------------------------------------------------------------------------
 template <int DIM, int JM, int G, bool DET, bool EX>
-__global__ void __launch_bounds__(512) y2k_coil_kernel(Geom g, const float2* __restrict__ y,
+__global__ void __launch_bounds__(DET ? 256 : 512) y2k_coil_kernel(Geom g, const float2* __restrict__ y,
                                                        float2* __restrict__ grid,
                                                        unsigned long long* __restrict__ igrid,
                                                        int bc, const double* __restrict__ dscal) {

@@ -180,7 +180,7 @@ static int y2k_launch(const Geom& g, const float2* y, float2* grid, unsigned lon
         bool exact = true;
         for (int d = 0; d < DIM; ++d) exact = exact && (g.J[d] == JM);
         kern = exact ? y2k_coil_kernel<DIM, JM, G, DET, true> : y2k_coil_kernel<DIM, JM, G, DET, false>;
-        threads = 512;
+        threads = DET ? 256 : 512;   // the 64-bit tiles of the exact mode need the registers
     }
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,

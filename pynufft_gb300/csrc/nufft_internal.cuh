@@ -112,9 +112,12 @@ struct nufft_plan_s {
     float2* d_ybuf = nullptr;         // M * B sample workspace (selfadjoint, CG)
     float2* d_maps = nullptr;         // coil sensitivities Nd x B (nufft_set_sense)
     int* d_kerr = nullptr;            // device error flag written by bounded waits
-    // optional CUDA-event timing of the k2y / y2k kernels (nufft_plan_kernel_timing)
+    // optional CUDA-event timing of the k2y / y2k kernels (nufft_plan_kernel_timing):
+    // events are created once and reused; kused[w] of kev[w] hold the records
+    // (start, stop, start, stop, ...) since timing was enabled
     bool ktime = false;
-    std::vector<cudaEvent_t> kev[2];  // [0] k2y, [1] y2k: start, stop, start, stop, ...
+    std::vector<cudaEvent_t> kev[2];  // [0] k2y, [1] y2k
+    size_t kused[2] = {0, 0};
     size_t ybuf_elems = 0;
 
     // point data (valid after nufft_set_points)
@@ -204,7 +207,8 @@ void free_points(nufft_plan_s* p);
 // interp.cu
 int launch_k2y(nufft_plan_s* p, const float2* grid, float2* y, cudaStream_t s);
 void kernel_time_mark(nufft_plan_s* p, int which, cudaStream_t s);
-void kernel_time_clear(nufft_plan_s* p);
+void kernel_time_clear(nufft_plan_s* p);     // forget the records, keep the events
+void kernel_time_destroy(nufft_plan_s* p);   // free the events
 int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s);
 
 // fftstage.cu
