@@ -279,9 +279,11 @@ def main():
         step()
     torch.cuda.synchronize()
     # the dominant kernels' own durations, from CUDA events the library
-    # records around each k2y / y2k launch on the launching stream during the
-    # timed steps
-    lib.nufft_plan_kernel_timing(A._plan, 1)
+    # records around every period-th k2y / y2k launch on the launching stream
+    # during the timed steps (about 20 samples spread over the timed region;
+    # an event pair around every launch costs short steps ~10%)
+    t_period = max(1, args.steps // 20)
+    lib.nufft_plan_kernel_timing(A._plan, t_period)
     clocks = ClockSampler(local)
     clocks.start()
     if dist:

@@ -118,13 +118,15 @@ int nufft_plan_set_bins(nufft_plan_t plan, const int* bin_shape, int max_sub_poi
 int nufft_plan_set_methods(nufft_plan_t plan, int k2y_method, int y2k_method);
 
 /* Optional timing of the interpolation (k2y) and gridding (y2k) kernels:
- * while enabled, every k2y / y2k kernel launch of this plan is bracketed by a
- * pair of CUDA events on its own stream (skipped while the stream is being
- * captured into a graph).  nufft_plan_kernel_times waits for the recorded
- * events and returns the summed kernel time (ms) and the number of launches
- * of each, then forgets them.  Enabling or disabling also forgets them.  No
- * counterpart in the reference. */
-int nufft_plan_kernel_timing(nufft_plan_t plan, int enable);
+ * with period n > 0, the 1st, (n+1)-th, (2n+1)-th ... k2y and y2k kernel
+ * launches of this plan are each bracketed by a pair of CUDA events on their
+ * own stream (skipped while the stream is being captured into a graph);
+ * period 0 turns timing off, a negative period is NUFFT_EINVAL.
+ * nufft_plan_kernel_times waits for the recorded events and returns the
+ * summed time (ms) and the number of timed launches of each, then forgets
+ * them.  Setting the period also forgets them.  No counterpart in the
+ * reference. */
+int nufft_plan_kernel_timing(nufft_plan_t plan, int period);
 int nufft_plan_kernel_times(nufft_plan_t plan, double* k2y_ms, int* k2y_launches,
                             double* y2k_ms, int* y2k_launches);
 

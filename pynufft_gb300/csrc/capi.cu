@@ -273,10 +273,14 @@ int nufft_plan_info(nufft_plan_t p, int64_t* M_total, int64_t* n_sub, int64_t* d
     return NUFFT_OK;
 }
 
-int nufft_plan_kernel_timing(nufft_plan_t p, int enable) {
+int nufft_plan_kernel_timing(nufft_plan_t p, int period) {
     NUFFT_TRY(need_plan(p, "nufft_plan_kernel_timing"));
+    if (period < 0) {
+        set_error("nufft_plan_kernel_timing: period must be >= 0");
+        return NUFFT_EINVAL;
+    }
     kernel_time_clear(p);
-    p->ktime = enable != 0;
+    p->kperiod = period;
     return NUFFT_OK;
 }
 

@@ -30,42 +30,52 @@ static int pick_jm(const nufft_plan_s* p) {
 // ---------------------------------------------------------------------------
 // k2y
 // ---------------------------------------------------------------------------
-// Optional kernel timing: an event pair recorded around each k2y / y2k
-// kernel launch on its own stream (not while the stream is being captured).
-void kernel_time_mark(nufft_plan_s* p, int which, cudaStream_t s) {
-    if (!p->ktime) return;
+// Optional kernel timing: an event pair recorded on its own stream around
+// every kperiod-th k2y / y2k kernel launch (not while the stream is being
+// captured).  Sampling keeps the events' own stream work off most launches.
+bool kernel_time_start(nufft_plan_s* p, int which, cudaStream_t s) {
+    if (p->kperiod <= 0) return false;
+    if (p->kseen[which]++ % (size_t)p->kperiod != 0) return false;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+        return false;
     std::vector<cudaEvent_t>& v = p->kev[which];
-    if (p->kused[which] == v.size()) {   // grow the pool (amortised: events are reused)
+    while (v.size() < p->kused[which] + 2) {   // grow the pool by a pair (events are reused)
         cudaEvent_t e;
-        if (cudaEventCreate(&e) != cudaSuccess) return;
+        if (cudaEventCreate(&e) != cudaSuccess) return false;
         v.push_back(e);
     }
     cudaEventRecord(v[p->kused[which]++], s);
+    return true;
 }
 
-void kernel_time_clear(nufft_plan_s* p) { p->kused[0] = p->kused[1] = 0; }
+void kernel_time_stop(nufft_plan_s* p, int which, cudaStream_t s, bool started) {
+    if (started) cudaEventRecord(p->kev[which][p->kused[which]++], s);
+}
+
+void kernel_time_clear(nufft_plan_s* p) {
+    for (int w = 0; w < 2; ++w) p->kused[w] = p->kseen[w] = 0;
+}
 
 void kernel_time_destroy(nufft_plan_s* p) {
     for (int w = 0; w < 2; ++w) {
         for (cudaEvent_t e : p->kev[w]) cudaEventDestroy(e);
         p->kev[w].clear();
-        p->kused[w] = 0;
     }
+    kernel_time_clear(p);
 }
 
 int launch_k2y(nufft_plan_s* p, const float2* grid, float2* y, cudaStream_t s) {
     if (p->M == 0) return NUFFT_OK;
     Geom g = p->geom();
     const int jm = pick_jm(p);
-    kernel_time_mark(p, 0, s);
+    const bool timed = kernel_time_start(p, 0, s);
     switch (p->ndim) {
         case 1: k2y_dim1(jm, g, grid, y, s); break;
         case 2: k2y_dim2(jm, g, grid, y, s); break;
         default: k2y_dim3(jm, g, grid, y, s); break;
     }
-    kernel_time_mark(p, 0, s);
+    kernel_time_stop(p, 0, s, timed);
     return check_launch("k2y_kernel");
 }
 
@@ -142,9 +152,9 @@ int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s) {
     if (!(p->flags & NUFFT_FLAG_DETERMINISTIC)) {
         NUFFT_CUDA_TRY(cudaMemsetAsync(grid, 0, sizeof(float2) * ncells, s));
         if (p->M == 0) return NUFFT_OK;
-        kernel_time_mark(p, 1, s);
+        const bool timed = kernel_time_start(p, 1, s);
         const int st = y2k_dim<false>(p, g, y, grid, nullptr, nullptr, s);
-        kernel_time_mark(p, 1, s);
+        kernel_time_stop(p, 1, s, timed);
         return st;
     }
     // deterministic: exact fixed-point accumulation, then one rounding to float

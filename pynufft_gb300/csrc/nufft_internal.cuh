@@ -113,11 +113,13 @@ struct nufft_plan_s {
     float2* d_maps = nullptr;         // coil sensitivities Nd x B (nufft_set_sense)
     int* d_kerr = nullptr;            // device error flag written by bounded waits
     // optional CUDA-event timing of the k2y / y2k kernels (nufft_plan_kernel_timing):
-    // events are created once and reused; kused[w] of kev[w] hold the records
-    // (start, stop, start, stop, ...) since timing was enabled
-    bool ktime = false;
+    // every kperiod-th launch (0: off) is bracketed; events are created once
+    // and reused; kused[w] of kev[w] hold the records (start, stop, ...) since
+    // timing was enabled, kseen[w] counts the launches
+    int kperiod = 0;
     std::vector<cudaEvent_t> kev[2];  // [0] k2y, [1] y2k
     size_t kused[2] = {0, 0};
+    size_t kseen[2] = {0, 0};
     size_t ybuf_elems = 0;
 
     // point data (valid after nufft_set_points)
@@ -206,7 +208,8 @@ void free_points(nufft_plan_s* p);
 
 // interp.cu
 int launch_k2y(nufft_plan_s* p, const float2* grid, float2* y, cudaStream_t s);
-void kernel_time_mark(nufft_plan_s* p, int which, cudaStream_t s);
+bool kernel_time_start(nufft_plan_s* p, int which, cudaStream_t s);  // true: this launch is timed
+void kernel_time_stop(nufft_plan_s* p, int which, cudaStream_t s, bool started);
 void kernel_time_clear(nufft_plan_s* p);     // forget the records, keep the events
 void kernel_time_destroy(nufft_plan_s* p);   // free the events
 int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s);

@@ -450,20 +450,28 @@ def test_odd_grids_and_mixed_J_match_oracle(NUFFT, Nd, Kd, Jd):
 
 
 def test_kernel_timing_counts_the_launches(NUFFT):
-    """nufft_plan_kernel_timing brackets every k2y / y2k kernel launch with
-    CUDA events: a forward and an adjoint give one timed launch of each."""
+    """nufft_plan_kernel_timing with period n brackets the 1st, (n+1)-th ...
+    k2y / y2k kernel launches with CUDA events: period 1 times every launch,
+    period 3 over five forward+adjoint pairs times launches 1 and 4."""
     import ctypes
     g = load_golden('plan_3d')
     A = NUFFT(0)
     A.plan(g['om'], _tup(g['Nd']), _tup(g['Kd']), _tup(g['Jd']))
     L, P = A._lib, A._plan
-    L.nufft_plan_kernel_timing(P, 1)
-    A.forward(g['x'])
-    A.adjoint(g['y'])
     km, ym = ctypes.c_double(), ctypes.c_double()
     kn, yn = ctypes.c_int(), ctypes.c_int()
-    assert L.nufft_plan_kernel_times(P, ctypes.byref(km), ctypes.byref(kn), ctypes.byref(ym),
-                                     ctypes.byref(yn)) == 0
+    for period, pairs, timed in [(1, 1, 1), (3, 5, 2), (1, 4, 4)]:
+        assert L.nufft_plan_kernel_timing(P, period) == 0
+        for _ in range(pairs):
+            A.forward(g['x'])
+            A.adjoint(g['y'])
+        assert L.nufft_plan_kernel_times(P, ctypes.byref(km), ctypes.byref(kn), ctypes.byref(ym),
+                                         ctypes.byref(yn)) == 0
+        assert kn.value == timed and yn.value == timed, (period, kn.value, yn.value)
+        assert km.value > 0 and ym.value > 0
+    assert L.nufft_plan_kernel_timing(P, -1) != 0
     L.nufft_plan_kernel_timing(P, 0)
-    assert kn.value == 1 and yn.value == 1
-    assert km.value > 0 and ym.value > 0
+    A.forward(g['x'])
+    L.nufft_plan_kernel_times(P, ctypes.byref(km), ctypes.byref(kn), ctypes.byref(ym),
+                              ctypes.byref(yn))
+    assert kn.value == 0 and yn.value == 0
