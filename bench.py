@@ -240,7 +240,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group('nccl', device_id=torch.device('cuda', local))
 
-    from pynufft_gb300 import NUFFT
+    from pynufft_gb300 import NUFFT, _lib
     c, om, x = workload(args.config)
     dev = torch.device('cuda', local)
     A = NUFFT(dev)
@@ -325,9 +325,15 @@ def main():
         ms = float(t.item())
     ms_per_step = ms / args.steps
     value = world * ninst * args.steps / (ms / 1e3)   # many-instance configs count instance pairs
-    # own kernels per step (cuFFT kernels are the library's): pad, k2y, y2k,
-    # crop; several coils add the two coil transposes
-    launches_per_step = 4 if (c['batch'] or 1) == 1 else 6
+    # own kernels per step (cuFFT kernels are the library's): with the own
+    # pruned FFT passes, one pass per axis each way plus k2y and y2k; else
+    # pad, k2y, y2k, crop, and with several coils the two coil transposes
+    fkind = c_int(-1)
+    lib.nufft_plan_transform_kind(A._plan, byref(fkind))
+    if fkind.value == _lib.NUFFT_FFT_OWN_PRUNED:
+        launches_per_step = 2 * len(c['Nd']) + 2
+    else:
+        launches_per_step = 4 if (c['batch'] or 1) == 1 else 6
 
     # dominant kernel alone: k2y and y2k, CUDA events on the launching stream
     def time_call(fn, reps=20):

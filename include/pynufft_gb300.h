@@ -46,6 +46,10 @@ extern "C" {
 
 /* ---- plan flags */
 #define NUFFT_FLAG_DETERMINISTIC 1  /* bitwise-reproducible gridding (y2k)    */
+#define NUFFT_FLAG_OWN_FFT       2  /* the library's own pruned power-of-two
+                                       FFT passes instead of cuFFT, where the
+                                       plan allows them (see
+                                       nufft_plan_transform_kind)             */
 
 typedef struct nufft_plan_s* nufft_plan_t;
 
@@ -154,6 +158,17 @@ int nufft_plan_check(nufft_plan_t plan, void* stream);
  * bytes of device memory the plan holds. */
 int nufft_plan_info(nufft_plan_t plan, int64_t* M_total, int64_t* n_subproblems,
                     int64_t* device_bytes);
+
+/* Which transform the image <-> spectrum stages of this plan run:
+ * NUFFT_FFT_CUFFT (cuFFT over the whole padded grid), NUFFT_FFT_CUFFT_PRUNED
+ * (cuFFT on the slabs the padding leaves nonzero), NUFFT_FFT_OWN_PRUNED (the
+ * library's pruned power-of-two passes: NUFFT_FLAG_OWN_FFT set, one coil,
+ * one instance, 2D/3D, Nd[0] < Kd[0], every Kd a power of two in 16..4096).
+ * No counterpart in the reference (numpy fftn / ifftn). */
+#define NUFFT_FFT_CUFFT        0
+#define NUFFT_FFT_CUFFT_PRUNED 1
+#define NUFFT_FFT_OWN_PRUNED   2
+int nufft_plan_transform_kind(nufft_plan_t plan, int* kind);
 
 /* ---- the six stages (nufft/__init__.py:658-692) ---------------------------
  * x2xx  (_x2xx_cpu  :224-230)  xx = x * sn                       Nd -> Nd

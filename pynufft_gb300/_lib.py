@@ -24,6 +24,8 @@ NUFFT_ECG_BREAKDOWN = 7
 NUFFT_EUNSUPPORTED = 8
 NUFFT_ETIMEOUT = 9
 NUFFT_FLAG_DETERMINISTIC = 1
+NUFFT_FLAG_OWN_FFT = 2
+NUFFT_FFT_CUFFT, NUFFT_FFT_CUFFT_PRUNED, NUFFT_FFT_OWN_PRUNED = 0, 1, 2
 NUFFT_K2Y_ZTEAM, NUFFT_K2Y_POINT, NUFFT_K2Y_TILE, NUFFT_K2Y_TILE_POINT = 1, 2, 3, 4
 NUFFT_Y2K_ZTEAM, NUFFT_Y2K_POINT, NUFFT_Y2K_GLOBAL = 1, 2, 3
 
@@ -40,6 +42,7 @@ SIGNATURES = {
     'nufft_plan_destroy': (c_int, [c_void_p]),
     'nufft_plan_set_bins': (c_int, [c_void_p, POINTER(c_int), c_int]),
     'nufft_plan_info': (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]),
+    'nufft_plan_transform_kind': (c_int, [c_void_p, POINTER(c_int)]),
     'nufft_plan_set_methods': (c_int, [c_void_p, c_int, c_int]),
     'nufft_x2xx': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     'nufft_xx2k': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -273,6 +273,17 @@ int nufft_plan_info(nufft_plan_t p, int64_t* M_total, int64_t* n_sub, int64_t* d
     return NUFFT_OK;
 }
 
+int nufft_plan_transform_kind(nufft_plan_t p, int* kind) {
+    NUFFT_TRY(need_plan(p, "nufft_plan_transform_kind"));
+    if (!kind) {
+        set_error("nufft_plan_transform_kind: NULL argument");
+        return NUFFT_EINVAL;
+    }
+    *kind = p->pfft ? NUFFT_FFT_OWN_PRUNED
+                    : (p->fft_pruned ? NUFFT_FFT_CUFFT_PRUNED : NUFFT_FFT_CUFFT);
+    return NUFFT_OK;
+}
+
 int nufft_plan_kernel_timing(nufft_plan_t p, int period) {
     NUFFT_TRY(need_plan(p, "nufft_plan_kernel_timing"));
     if (period < 0) {
@@ -363,10 +374,10 @@ int nufft_k2xx(nufft_plan_t p, const void* k, void* xx, void* stream) {
     NUFFT_TRY(need_ptrs(k, xx, "nufft_k2xx"));
     cudaStream_t s = as_stream(stream);
     if (p->B > 1) return image_from_spectrum_coils(p, (const float2*)k, (float2*)xx, false, false, s);
+    if (p->pfft) return image_from_spectrum(p, (const float2*)k, (float2*)xx, false, false, s);
     const size_t n = (size_t)p->ninst * p->prodK * p->B;
     NUFFT_CUDA_TRY(cudaMemcpyAsync(p->d_grid, k, sizeof(float2) * n, cudaMemcpyDeviceToDevice, s));
-    NUFFT_TRY(fft_exec(p, p->d_grid, +1, s));
-    return launch_crop(p, p->d_grid, (float2*)xx, false, false, s);
+    return image_from_spectrum(p, p->d_grid, (float2*)xx, false, false, s);
 }
 
 int nufft_k2y(nufft_plan_t p, const void* k, void* y, void* stream) {
@@ -395,8 +406,7 @@ int nufft_adjoint(nufft_plan_t p, const void* y, void* x, void* stream) {
     cudaStream_t s = as_stream(stream);
     NUFFT_TRY(launch_y2k(p, (const float2*)y, p->d_grid, s));
     if (p->B > 1) return image_from_spectrum_coils(p, p->d_grid, (float2*)x, true, false, s);
-    NUFFT_TRY(fft_exec(p, p->d_grid, +1, s));
-    return launch_crop(p, p->d_grid, (float2*)x, true, false, s);
+    return image_from_spectrum(p, p->d_grid, (float2*)x, true, false, s);
 }
 
 int nufft_selfadjoint(nufft_plan_t p, const void* x, void* x_out, void* stream) {

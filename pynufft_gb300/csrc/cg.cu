@@ -385,8 +385,7 @@ int solve_cg(nufft_plan_s* p, const float2* y, float2* x, int maxiter, double rt
 
     // k-space solution -> image: k2xx then divide by sn
     float2* xk = p->d_cg;
-    NUFFT_TRY(fft_exec(p, xk, +1, s));
-    NUFFT_TRY(launch_crop(p, xk, x, false, true, s));
+    NUFFT_TRY(image_from_spectrum(p, xk, x, false, true, s));
 
     if (iters_out) {
         NUFFT_CUDA_TRY(cudaMemcpyAsync(hs.data(), p->d_cgs, sizeof(CGSys) * g.S,

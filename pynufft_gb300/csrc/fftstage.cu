@@ -486,6 +486,7 @@ int forward_from_image(nufft_plan_s* p, const float2* xx, bool apply_sn, float2*
         NUFFT_TRY(fft_cm_exec(p, -1, s));
         return coil_transpose(p, p->d_cm, k, false, s);
     }
+    if (p->pfft) return pfft_forward(p, xx, apply_sn, k, s);
     if (!(p->fft_pruned && p->d_padin)) {
         NUFFT_TRY(launch_pad(p, xx, k, apply_sn, -1, s));
         return fft_exec(p, k, -1, s);
@@ -508,6 +509,16 @@ int forward_from_image(nufft_plan_s* p, const float2* xx, bool apply_sn, float2*
     NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_slab, a, b, CUFFT_FORWARD));
     NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_x, b, kc, CUFFT_FORWARD));
     return NUFFT_OK;
+}
+
+// One coil: the own pruned passes, else the inverse cuFFT in place on k
+// followed by the crop.
+int image_from_spectrum(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn,
+                        bool divide_sn, cudaStream_t s) {
+    if (p->pfft) return pfft_inverse(p, k, xx, apply_sn, divide_sn, s);
+    float2* kk = const_cast<float2*>(k);
+    NUFFT_TRY(fft_exec(p, kk, +1, s));
+    return launch_crop(p, kk, xx, apply_sn, divide_sn, s);
 }
 
 int launch_crop(const nufft_plan_s* p, const float2* grid, float2* xx, bool apply_sn,
@@ -670,7 +681,9 @@ int fft_init(nufft_plan_s* p) {
         NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_slab, p->d_fftwork));
         NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_x, p->d_fftwork));
     }
-    return NUFFT_OK;
+    // own pruned passes where the grid allows (they use d_padin / d_slabout
+    // as their intermediate arrays)
+    return pfft_init(p);
 }
 
 void fft_destroy(nufft_plan_s* p) {
@@ -680,6 +693,7 @@ void fft_destroy(nufft_plan_s* p) {
         cufftDestroy(p->fft_x);
     }
     p->fft_ok = p->fft_pruned = p->fft_cm_pruned = false;
+    pfft_free(p);
     cudaFree(p->d_fftwork);
     p->d_fftwork = nullptr;
     cudaFree(p->d_padin);

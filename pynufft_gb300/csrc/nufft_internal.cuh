@@ -158,6 +158,9 @@ struct nufft_plan_s {
     void* d_fftwork = nullptr;        // shared cuFFT work area
     float2* d_padin = nullptr;        // pruned forward: zero-padded input, first Nd[0] slabs
     float2* d_slabout = nullptr;      // pruned forward: slab-FFT output, other slabs zero
+    bool pfft = false;                // own pruned power-of-two FFT passes (pfft.cu)
+    float2* d_pfft_tw = nullptr;      // per-axis, per-stage twiddle tables, concatenated
+    int pfft_tw_off[3][4] = {};       // [axis][stage] offsets into d_pfft_tw
     float2* d_cm = nullptr;           // B > 1: coil-major copy of the grid for the FFTs
     size_t dev_bytes = 0;
 
@@ -229,6 +232,17 @@ int launch_pad_sense(const nufft_plan_s* p, const float2* x, float2* grid, cudaS
 int launch_crop_sense(const nufft_plan_s* p, const float2* grid, float2* x, cudaStream_t s);
 int fft_init(nufft_plan_s* p);
 void fft_destroy(nufft_plan_s* p);
+// k (Kd) -> image: inverse transform, crop, / prod(Kd), x sn or / sn (B == 1)
+int image_from_spectrum(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn,
+                        bool divide_sn, cudaStream_t s);
+
+// pfft.cu: own pruned power-of-two FFT passes (B == 1, one instance)
+bool pfft_eligible(const nufft_plan_s* p);
+int pfft_init(nufft_plan_s* p);
+void pfft_free(nufft_plan_s* p);
+int pfft_forward(nufft_plan_s* p, const float2* x, bool apply_sn, float2* k, cudaStream_t s);
+int pfft_inverse(nufft_plan_s* p, const float2* k, float2* x, bool apply_sn, bool divide_sn,
+                 cudaStream_t s);
 
 // cg.cu
 int solve_cg(nufft_plan_s* p, const float2* y, float2* x, int maxiter, double rtol,

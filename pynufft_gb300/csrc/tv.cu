@@ -199,8 +199,7 @@ int solve_l1tvols(nufft_plan_s* p, const float2* y, float2* x, int maxiter, doub
             NUFFT_TRY(forward_from_image(p, rhs, false, p->d_grid, s));
             tv_kdiv_kernel<<<gk, 256, 0, s>>>(p->d_grid, uker, nk);
             NUFFT_CUDA_TRY(cudaGetLastError());
-            NUFFT_TRY(fft_exec(p, p->d_grid, +1, s));
-            NUFFT_TRY(launch_crop(p, p->d_grid, x, false, false, s));
+            NUFFT_TRY(image_from_spectrum(p, p->d_grid, x, false, false, s));
             tv_shrink_kernel<<<gi, 256, 0, s>>>(d, x, dd, bb, (float)(1.0 / rho));
             NUFFT_CUDA_TRY(cudaGetLastError());
             NUFFT_TRY(nufft_selfadjoint(p, x, aha, s));

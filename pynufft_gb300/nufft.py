@@ -64,7 +64,7 @@ class NUFFT:
 
     # ------------------------------------------------------------------ plan
     def plan(self, om, Nd, Kd, Jd, ft_axes=None, batch=None, deterministic=False,
-             bins=None, max_sub_points=None, autotune=False):
+             bins=None, max_sub_points=None, autotune=False, fft='cufft'):
         """Plan for the points ``om`` (M x ndim radians).
 
         Argument checks follow helper.plan (src/_helper/helper.py:644-654):
@@ -73,9 +73,14 @@ class NUFFT:
         gridding mode.  ``bins``/``max_sub_points`` override the gridding bin
         shape; ``autotune=True`` applies the cached best setting for this
         geometry and point density, or searches once (``pynufft_gb300.autotune``).
-        Returns 0.
+        ``fft='own'`` runs the image <-> spectrum transforms through the
+        library's own pruned power-of-two passes where the plan allows them
+        (one coil, 2D/3D, every Kd a power of two); the default ``'cufft'``
+        uses cuFFT, faster on this GPU.  Returns 0.
         """
         self._check_shapes(Nd, Kd, Jd)
+        if fft not in ('cufft', 'own'):
+            raise ValueError("fft must be 'cufft' or 'own'")
         ndim = len(Nd)
         if ft_axes is not None and tuple(sorted(ft_axes)) != tuple(range(ndim)):
             raise NotImplementedError('pynufft_gb300 transforms over all axes (ft_axes=None)')
@@ -83,7 +88,7 @@ class NUFFT:
         if B < 1:
             raise ValueError('batch must be a positive integer')
         st = self._plan_common([om], Nd, Kd, Jd, batch, B, 1, deterministic, bins,
-                               max_sub_points)
+                               max_sub_points, fft)
         if autotune:
             self._autotune([om])
         return st
@@ -125,10 +130,13 @@ class NUFFT:
             raise KeyError('Nd, Kd, Jd must be in the same length, e.g. '
                            'Nd=(256,256),Kd=(512,512),Jd=(6,6)')
 
-    def _plan_common(self, oms, Nd, Kd, Jd, batch, B, ninst, deterministic, bins, max_sub):
+    def _plan_common(self, oms, Nd, Kd, Jd, batch, B, ninst, deterministic, bins, max_sub,
+                     fft='cufft'):
         torch = _torch()
         ndim = len(Nd)
         flags = _lib.NUFFT_FLAG_DETERMINISTIC if deterministic else 0
+        if fft == 'own':
+            flags |= _lib.NUFFT_FLAG_OWN_FFT
         key = (tuple(Nd), tuple(Kd), tuple(Jd), B, ninst, flags,
                None if bins is None else tuple(bins), max_sub)
         reuse = (self._plan is not None and getattr(self, '_key', None) == key
