@@ -13,8 +13,8 @@ Prints ONE JSON line (rank 0).  `value` times steps with inputs resident on
 the device (CUDA events on the launching stream); `e2e` times the public API
 (`NUFFT.forward`/`adjoint` on pinned host tensors, copies included);
 `roofline` uses the dominant kernel's own average duration, from CUDA events
-that the library records around each of its launches on the launching stream
-during the timed steps;
+that the library records around every n-th of its launches (about 20 spread
+over the timed steps) on the launching stream;
 `cpu_baseline` times the CPU oracle (a restatement of the reference numpy
 path) on a bounded sample.  With --gpus N > 1 (torchrun) every rank runs an
 independent replica of the workload (no collective on the data path) and
