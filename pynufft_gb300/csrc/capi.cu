@@ -173,6 +173,17 @@ int nufft_plan_create(int ndim, const int* Nd, const int* Kd, const int* Jd, int
         return fail(e == cudaErrorMemoryAllocation ? NUFFT_ENOMEM : NUFFT_ECUDA);
     }
     p->dev_bytes = sizeof(float) * sumN + sizeof(AxisConst) * 3 + sizeof(float2) * ncell;
+    if (batch == 1 && ninst == 1 && !(flags & NUFFT_FLAG_DETERMINISTIC)) {
+        e = cudaMalloc(&p->d_grid_adj, sizeof(float2) * ncell);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->zs, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_zero, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_adj, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            set_error(std::string("nufft_plan_create: ") + cudaGetErrorString(e));
+            return fail(e == cudaErrorMemoryAllocation ? NUFFT_ENOMEM : NUFFT_ECUDA);
+        }
+        p->dev_bytes += sizeof(float2) * ncell;
+    }
     int st = fft_init(p);
     if (st != NUFFT_OK) return fail(st);
     *plan_out = p;
@@ -187,6 +198,11 @@ int nufft_plan_destroy(nufft_plan_t p) {
     cudaFree(p->d_snd);
     cudaFree(p->d_axc);
     cudaFree(p->d_grid);
+    if (p->zs) cudaStreamSynchronize(p->zs);
+    cudaFree(p->d_grid_adj);
+    if (p->ev_zero) cudaEventDestroy(p->ev_zero);
+    if (p->ev_adj) cudaEventDestroy(p->ev_adj);
+    if (p->zs) cudaStreamDestroy(p->zs);
     cudaFree(p->d_igrid);
     cudaFree(p->d_dscal);
     cudaFree(p->d_maps);
@@ -392,10 +408,23 @@ int nufft_y2k(nufft_plan_t p, const void* y, void* k, void* stream) {
     return launch_y2k(p, (const float2*)y, (float2*)k, as_stream(stream));
 }
 
+static bool capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
+}
+
 int nufft_forward(nufft_plan_t p, const void* x, void* y, void* stream) {
     NUFFT_TRY(need_points(p, "nufft_forward"));
     NUFFT_TRY(need_ptrs(x, y, "nufft_forward", p));
     cudaStream_t s = as_stream(stream);
+    if (p->d_grid_adj && !p->adj_zeroed && !capturing(s)) {
+        // zero the adjoint's grid on the side stream, after the last adjoint
+        // has read it, while this forward runs
+        if (p->adj_used) NUFFT_CUDA_TRY(cudaStreamWaitEvent(p->zs, p->ev_adj, 0));
+        NUFFT_CUDA_TRY(cudaMemsetAsync(p->d_grid_adj, 0, sizeof(float2) * p->prodK, p->zs));
+        NUFFT_CUDA_TRY(cudaEventRecord(p->ev_zero, p->zs));
+        p->adj_zeroed = true;
+    }
     NUFFT_TRY(forward_from_image(p, (const float2*)x, true, p->d_grid, s));
     return launch_k2y(p, p->d_grid, (float2*)y, s);
 }
@@ -404,6 +433,19 @@ int nufft_adjoint(nufft_plan_t p, const void* y, void* x, void* stream) {
     NUFFT_TRY(need_points(p, "nufft_adjoint"));
     NUFFT_TRY(need_ptrs(x, y, "nufft_adjoint", p));
     cudaStream_t s = as_stream(stream);
+    if (p->d_grid_adj && !capturing(s)) {
+        bool pre = false;
+        if (p->adj_zeroed) {
+            NUFFT_CUDA_TRY(cudaStreamWaitEvent(s, p->ev_zero, 0));
+            pre = true;
+        }
+        p->adj_zeroed = false;   // consumed (or zeroed inline below)
+        NUFFT_TRY(launch_y2k(p, (const float2*)y, p->d_grid_adj, s, pre));
+        const int st = image_from_spectrum(p, p->d_grid_adj, (float2*)x, true, false, s);
+        NUFFT_CUDA_TRY(cudaEventRecord(p->ev_adj, s));
+        p->adj_used = true;
+        return st;
+    }
     NUFFT_TRY(launch_y2k(p, (const float2*)y, p->d_grid, s));
     if (p->B > 1) return image_from_spectrum_coils(p, p->d_grid, (float2*)x, true, false, s);
     return image_from_spectrum(p, p->d_grid, (float2*)x, true, false, s);

@@ -146,11 +146,11 @@ static int y2k_dim(const nufft_plan_s* p, const Geom& g, const float2* y, float2
     }
 }
 
-int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s) {
+int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s, bool pre_zeroed) {
     const size_t ncells = (size_t)p->ninst * p->prodK * p->B;
     Geom g = p->geom();
     if (!(p->flags & NUFFT_FLAG_DETERMINISTIC)) {
-        NUFFT_CUDA_TRY(cudaMemsetAsync(grid, 0, sizeof(float2) * ncells, s));
+        if (!pre_zeroed) NUFFT_CUDA_TRY(cudaMemsetAsync(grid, 0, sizeof(float2) * ncells, s));
         if (p->M == 0) return NUFFT_OK;
         const bool timed = kernel_time_start(p, 1, s);
         const int st = y2k_dim<false>(p, g, y, grid, nullptr, nullptr, s);

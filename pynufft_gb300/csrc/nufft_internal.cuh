@@ -109,6 +109,14 @@ struct nufft_plan_s {
     float* d_snd = nullptr;           // per-axis scaling factors (float32), concatenated
     nufft::AxisConst* d_axc = nullptr;
     float2* d_grid = nullptr;         // ninst * prodK * B oversampled grid workspace
+    // adjoint's own grid (one coil, one instance, fast gridding): zeroed on a
+    // side stream while the forward runs, so the adjoint's gridding needs no
+    // memset on its own path; ev_zero marks the zeroing done, ev_adj the
+    // last adjoint's reads of it done
+    float2* d_grid_adj = nullptr;
+    cudaStream_t zs = nullptr;
+    cudaEvent_t ev_zero = nullptr, ev_adj = nullptr;
+    bool adj_zeroed = false, adj_used = false;
     float2* d_ybuf = nullptr;         // M * B sample workspace (selfadjoint, CG)
     float2* d_maps = nullptr;         // coil sensitivities Nd x B (nufft_set_sense)
     int* d_kerr = nullptr;            // device error flag written by bounded waits
@@ -215,7 +223,8 @@ bool kernel_time_start(nufft_plan_s* p, int which, cudaStream_t s);  // true: th
 void kernel_time_stop(nufft_plan_s* p, int which, cudaStream_t s, bool started);
 void kernel_time_clear(nufft_plan_s* p);     // forget the records, keep the events
 void kernel_time_destroy(nufft_plan_s* p);   // free the events
-int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s);
+int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s,
+               bool pre_zeroed = false);   // pre_zeroed: grid already zero (fast mode)
 
 // fftstage.cu
 int launch_scale(const nufft_plan_s* p, const float2* in, float2* out, cudaStream_t s);
