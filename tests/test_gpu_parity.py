@@ -475,3 +475,32 @@ def test_kernel_timing_counts_the_launches(NUFFT):
     L.nufft_plan_kernel_times(P, ctypes.byref(km), ctypes.byref(kn), ctypes.byref(ym),
                               ctypes.byref(yn))
     assert kn.value == 0 and yn.value == 0
+
+
+def test_adjoint_grid_zeroed_ahead_across_streams(NUFFT):
+    """One-coil plans zero the adjoint's grid on a side stream during the
+    forward: adjoints after a forward on another stream, repeated adjoints
+    (zeroed inline) and a selfadjoint all match the oracle."""
+    import torch
+    g = load_golden('plan_3d')
+    A = NUFFT(0)
+    A.plan(g['om'], _tup(g['Nd']), _tup(g['Kd']), _tup(g['Jd']))
+    O = OracleNUFFT()
+    O.plan(g['om'], _tup(g['Nd']), _tup(g['Kd']), _tup(g['Jd']))
+    ref_y, ref_x = O.forward(g['x']), O.adjoint(g['y'])
+    xd = torch.from_numpy(g['x']).cuda()
+    yd = torch.from_numpy(g['y']).cuda()
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    for _ in range(3):
+        with torch.cuda.stream(s1):
+            yo = A.forward(xd)
+        s2.wait_stream(s1)
+        with torch.cuda.stream(s2):
+            xo = A.adjoint(yd)
+            xo2 = A.adjoint(yd)
+        torch.cuda.synchronize()
+        assert rel_l2(yo.cpu().numpy(), ref_y) < TOL
+        assert rel_l2(xo.cpu().numpy(), ref_x) < TOL
+        assert rel_l2(xo2.cpu().numpy(), ref_x) < TOL
+    assert rel_l2(A.selfadjoint(g['x']), O.selfadjoint(g['x'])) < TOL
+    A.check()
