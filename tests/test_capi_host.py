@@ -31,6 +31,20 @@ def test_library_exports_every_declared_symbol():
     assert b'sm_103a' in lib.nufft_version()
 
 
+def test_python_constants_match_the_header():
+    """Every NUFFT_* integer constant the Python binding mirrors has the
+    header's value (status codes, plan flags, method and transform kinds)."""
+    from pynufft_gb300 import _lib
+    src = re.sub(r'/\*.*?\*/', '', open(HEADER).read(), flags=re.S)
+    defs = {m.group(1): int(m.group(2))
+            for m in re.finditer(r'#define\s+(NUFFT_[A-Z0-9_]+)\s+(-?\d+)', src)}
+    mirrored = [n for n in dir(_lib) if n.startswith('NUFFT_') and isinstance(getattr(_lib, n), int)]
+    assert len(mirrored) >= 15
+    for n in mirrored:
+        assert n in defs, n
+        assert getattr(_lib, n) == defs[n], (n, getattr(_lib, n), defs[n])
+
+
 def _axis(N, J, K, alpha_in=None):
     from pynufft_gb300 import _lib
     lib = _lib.load()
