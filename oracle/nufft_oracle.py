@@ -202,7 +202,11 @@ class OracleNUFFT:
     single-coil transform sharing the plan.
     """
 
-    def plan(self, om, Nd, Kd, Jd, batch=None, threads=1):
+    def plan(self, om, Nd, Kd, Jd, batch=None, threads=1, build_threads=None):
+        """``threads``: host threads of the sparse products and FFTs (1 = the
+        reference's single-threaded numpy/scipy calls).  ``build_threads``
+        (default ``threads``): threads that build the CSR matrices, on row
+        chunks whose stacked result is identical to the one-piece build."""
         check_plan_args(Nd, Kd, Jd)
         self.Nd, self.Kd, self.Jd = Nd, Kd, Jd
         self.ndims = len(Nd)
@@ -218,8 +222,22 @@ class OracleNUFFT:
             shp[i] = s.size
             sn = sn * s.reshape(shp)
         self.sn = np.asarray(sn.real.astype(np.complex64), order='C')
-        self.sp = interp_csr(om, Nd, Kd, Jd, self.params)
-        self.spH = self.sp.getH().tocsr()
+        nb = int(build_threads or self.threads)
+        if nb <= 1 or self.M < 2 * 65536:
+            self.sp = interp_csr(om, Nd, Kd, Jd, self.params)
+            self.spH = self.sp.getH().tocsr()
+        else:
+            edges = np.linspace(0, self.M, 4 * nb + 1).astype(np.int64)
+            spans = [(int(a), int(b)) for a, b in zip(edges[:-1], edges[1:]) if b > a]
+
+            def part(ab):
+                a, b = ab
+                sp = interp_csr(om[a:b], Nd, Kd, Jd, self.params)
+                return sp, sp.getH().tocsr()
+            with ThreadPoolExecutor(nb) as ex:
+                parts = list(ex.map(part, spans))
+            self.sp = scipy.sparse.vstack([p[0] for p in parts], format='csr')
+            self.spH = scipy.sparse.hstack([p[1] for p in parts], format='csr')
         self._row_chunks = None
         return 0
 
@@ -380,7 +398,7 @@ class OracleNUFFT:
         return x
 
     def solve(self, y, solver='cg', maxiter=None, rtol=1e-5, atol=0.0,
-              return_info=False):
+              return_info=False, solver_kw=None, operator_dtype=None):
         """solve(y, 'cg', maxiter): CG on the k-space normal operator spH.sp,
         x0 = 0, then k2xx(k) / sn (linalg/solve_cpu.py:256-288).  The CG
         recursion restates scipy.sparse.linalg.cg (scipy 1.18.1,
@@ -398,13 +416,28 @@ class OracleNUFFT:
                 if solver == 'lsmr' else fn(self.sp, np.asarray(y).ravel(), iter_lim=maxiter, **kw)[0]
             xx = self._k2xx1(np.reshape(k, self.Kd))
             return xx / self.sn
+        if solver in ('bicg', 'bicgstab', 'gmres', 'lgmres'):
+            # linalg/solve_cpu.py:253-288: the scipy routine on the Hermitian
+            # normal operator spH.sp (k2y2k), b = y2k(y), then k2xx(k) / sn
+            import scipy.sparse.linalg as sla
+            n = int(np.prod(self.Kd))
+
+            def spHsp(v):
+                return self._matvec(self.spH, self._matvec(self.sp, v))
+            A = sla.LinearOperator((n, n), matvec=spHsp, rmatvec=spHsp, dtype=np.complex128)
+            b = np.reshape(self._y2k1(y), (-1,))
+            kw = dict(rtol=rtol, atol=atol, maxiter=maxiter, **(solver_kw or {}))
+            k, info = getattr(sla, solver)(A, b, **kw)
+            xx = self._k2xx1(np.reshape(k, self.Kd))
+            return (xx / self.sn, info) if return_info else xx / self.sn
         if solver != 'cg':
             raise NotImplementedError(solver)
 
         def one(yc):
             b = np.reshape(self._y2k1(yc), (-1,))
             x, it = cg_restated(lambda v: self._matvec(self.spH, self._matvec(self.sp, v)),
-                                b, maxiter=maxiter, rtol=rtol, atol=atol)
+                                b, maxiter=maxiter, rtol=rtol, atol=atol,
+                                operator_dtype=operator_dtype)
             xx = self._k2xx1(np.reshape(x, self.Kd))
             return xx / self.sn, it
 
@@ -416,10 +449,80 @@ class OracleNUFFT:
         return (x, [o[1] for o in outs]) if return_info else x
 
 
-def cg_restated(matvec, b, maxiter=None, rtol=1e-5, atol=0.0):
+class ChunkedOracleNUFFT(OracleNUFFT):
+    """The reference numpy path planned on row chunks of ``om``, for point
+    sets whose full CSR does not fit in host memory (a 3D J=6 plan holds
+    216 complex128 entries per point, twice with ``spH``).
+
+    Rows of the interpolation matrix are independent, so ``k2y`` is the
+    concatenation of each chunk's ``sp . k`` and ``y2k`` the sum of each
+    chunk's ``spH . y`` (nufft/_nufft_class_methods_cpu.py:273-314); the
+    FFT and scaling stages are the unchunked ones.  A chunk's CSR is built
+    when it is used and dropped afterwards.  ``k2y_rows`` evaluates only the
+    selected rows (one CSR of those rows).
+    """
+
+    def plan(self, om, Nd, Kd, Jd, batch=None, threads=1, chunk=1_000_000):
+        check_plan_args(Nd, Kd, Jd)
+        self.Nd, self.Kd, self.Jd = Nd, Kd, Jd
+        self.ndims = len(Nd)
+        self.batch = batch
+        self.threads = int(threads)
+        self.om = np.asarray(om, dtype=np.float64)
+        self.M = self.om.shape[0]
+        self.chunk = int(chunk)
+        self.params = [alpha_beta_fit(Nd[i], Jd[i], Kd[i]) for i in range(self.ndims)]
+        self.snd = [scale_axis(Nd[i], Kd[i], *self.params[i]) for i in range(self.ndims)]
+        sn = np.ones(())
+        for i, s in enumerate(self.snd):
+            shp = [1] * self.ndims
+            shp[i] = s.size
+            sn = sn * s.reshape(shp)
+        self.sn = np.asarray(sn.real.astype(np.complex64), order='C')
+        self._row_chunks = None
+        return 0
+
+    def _csr(self, a, b):
+        return interp_csr(self.om[a:b], self.Nd, self.Kd, self.Jd, self.params)
+
+    def _k2y1(self, k):
+        kv = np.reshape(k, (-1,))
+        out = np.empty(self.M, dtype=np.complex128)
+        for a in range(0, self.M, self.chunk):
+            b = min(self.M, a + self.chunk)
+            out[a:b] = self._csr(a, b).dot(kv)
+        return out
+
+    def _y2k1(self, y):
+        acc = np.zeros(int(np.prod(self.Kd)), dtype=np.complex128)
+        for a in range(0, self.M, self.chunk):
+            b = min(self.M, a + self.chunk)
+            acc += self._csr(a, b).getH().dot(y[a:b])
+        return np.reshape(acc, self.Kd)
+
+    def k2y_rows(self, k, rows):
+        """k2y at the selected rows only: (len(rows),) or (len(rows), B)."""
+        rows = np.asarray(rows)
+        sp = interp_csr(self.om[rows], self.Nd, self.Kd, self.Jd, self.params)
+        if self.batch is None:
+            return sp.dot(np.reshape(k, (-1,)))
+        return np.stack([sp.dot(np.reshape(k[..., b], (-1,))) for b in range(k.shape[-1])], -1)
+
+    def forward_rows(self, x, rows):
+        """forward(x) at the selected rows: k = xx2k(x2xx(x)) on the full
+        grid, then the interpolation rows."""
+        return self.k2y_rows(self.xx2k(self.x2xx(x)), rows)
+
+
+def cg_restated(matvec, b, maxiter=None, rtol=1e-5, atol=0.0, operator_dtype=None):
     """Conjugate gradients with scipy.sparse.linalg.cg's recursion and stopping
     rule (x0 = 0; stop when ||r|| < max(atol, rtol*||b||) at the top of an
-    iteration).  Returns (x, iterations_run)."""
+    iteration).  Returns (x, iterations_run).
+
+    ``operator_dtype`` (e.g. numpy.complex64) rounds the operator's input and
+    output to that type, everything else staying complex128: the recursion
+    as run with a single-precision operator.  Tests use it to measure how far
+    any float32 operator's CG iterates drift from the complex128 ones."""
     b = np.asarray(b)
     bnrm2 = np.linalg.norm(b)
     tol = max(float(atol), float(rtol) * float(bnrm2))
@@ -439,7 +542,10 @@ def cg_restated(matvec, b, maxiter=None, rtol=1e-5, atol=0.0):
             p = r + (rho / rho_prev) * p
         else:
             p = r.copy()
-        q = matvec(p)
+        if operator_dtype is None:
+            q = matvec(p)
+        else:
+            q = matvec(p.astype(operator_dtype).astype(b.dtype)).astype(operator_dtype).astype(b.dtype)
         alpha = rho / np.vdot(p, q)
         x = x + alpha * p
         r = r - alpha * q
@@ -456,35 +562,41 @@ def _centred_grid(Nd):
 
 def nudft_forward_rows(x, om, rows=None):
     """y_m = sum_n x_n exp(-i om_m . (n - N/2)) for the selected rows, FP64.
-    Separable per axis, so memory is O(rows * sum(Nd))."""
+
+    Separable per axis: the innermost image axis is contracted for all rows by
+    one matrix product, the others by per-row weighted sums, so memory is
+    O(prod(Nd[:-1]) * rows) and the heavy step runs in BLAS."""
     x = np.asarray(x, dtype=np.complex128)
     om = np.asarray(om, dtype=np.float64)
     if rows is not None:
         om = om[np.asarray(rows)]
     Nd = x.shape
+    nd = len(Nd)
     grids = _centred_grid(Nd)
-    F = [np.exp(-1j * np.outer(om[:, d], grids[d])) for d in range(len(Nd))]
+    F = [np.exp(-1j * np.outer(om[:, d], grids[d])) for d in range(nd)]   # R x N_d
     out = np.empty(om.shape[0], dtype=np.complex128)
-    for s in range(0, om.shape[0], 256):
-        e = min(om.shape[0], s + 256)
-        t = x
-        # contract the last axis first, keeping the point axis in front
-        t = np.einsum('...n,mn->m...', t, F[-1][s:e])
-        for d in range(len(Nd) - 2, -1, -1):
-            t = np.einsum('m...n,mn->m...', t, F[d][s:e])
-        out[s:e] = t
+    step = 512
+    for s in range(0, om.shape[0], step):
+        e = min(om.shape[0], s + step)
+        # (prod(Nd[:-1]), N_last) @ (N_last, R) -> rows last
+        t = x.reshape(-1, Nd[-1]) @ F[-1][s:e].T
+        for d in range(nd - 2, -1, -1):
+            t = t.reshape(-1, Nd[d], e - s)
+            t = np.einsum('anr,rn->ar', t, F[d][s:e])
+        out[s:e] = t.reshape(e - s)
     return out
 
 
 def nudft_adjoint_pixels(y, om, Nd, pixels, chunk=65536):
     """x_n = sum_m y_m exp(+i om_m . (n - N/2)) at the selected flat pixel
     indices (C order), FP64, unnormalised, summed over chunks of points.  The
-    reference NUFFT adjoint equals this divided by prod(Kd)."""
+    reference NUFFT adjoint equals this divided by prod(Kd).  y may carry a
+    trailing coil axis (M, B); the result is then (pixels, B)."""
     y = np.asarray(y, dtype=np.complex128)
     om = np.asarray(om, dtype=np.float64)
     idx = np.unravel_index(np.asarray(pixels), Nd)
     cen = np.stack([idx[d] - Nd[d] / 2 for d in range(len(Nd))], 1)   # P x d
-    out = np.zeros(len(pixels), dtype=np.complex128)
+    out = np.zeros((len(pixels),) + y.shape[1:], dtype=np.complex128)
     for s in range(0, om.shape[0], chunk):
         e = min(om.shape[0], s + chunk)
         out += np.exp(1j * (cen @ om[s:e].T)) @ y[s:e]

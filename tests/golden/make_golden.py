@@ -1,11 +1,12 @@
 """Generate the golden fixtures in this directory from the reference itself.
 
-Run in a container that has the reference checked out at /root/reference:
+Run where a checkout of the reference (pynufft 2025.2.1) is available, giving
+its location with --reference or the PYNUFFT_REFERENCE environment variable:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference /path/to/pynufft [groups...]
 
 It imports the reference package read-only through a symlink
-(/tmp/refpkg/pynufft -> /root/reference, no bytecode written), runs the
+(<tmp>/refpkg/pynufft -> the checkout, no bytecode written), runs the
 reference numpy ``NUFFT`` on seeded synthetic inputs and writes ``*.npz``
 fixtures next to this script.  The GPU machine never runs this script; it only
 reads the fixtures.
@@ -17,6 +18,9 @@ Cases (all seeds fixed):
   radial_c1.npz  2D radial 256 spokes x 512 samples, Nd 256^2, Kd 512^2,
                Jd 6^2: reference forward at 4096 sampled rows and adjoint at
                4096 sampled pixels (inputs regenerated from their seeds).
+  cg_c1.npz    solve(y, 'cg', maxiter=20) of the reference on the radial_c1
+               plan, y = complex Gaussian samples (seed 100, the radial_c1
+               adjoint input): the full complex64 image.
   ndft_known_answer.npz  the exact-NDFT vectors shipped with the reference
                (tests/tmp2d_{1,2,3}_.mat: image fhat, points x, NDFT f2) and
                the reference's own J=6, K=2N forward at om = 2*pi*x.
@@ -24,7 +28,7 @@ Cases (all seeds fixed):
                radial plan (Nd 32^2) and a 3D random plan (Nd 12^3), y the
                reference forward of a disk phantom plus 1% noise.
 
-Pass case groups (plans, radial, ndft, l1tvols) to regenerate only those.
+Pass case groups (plans, radial, cg, ndft, l1tvols) to regenerate only those.
 """
 from __future__ import annotations
 
@@ -35,17 +39,21 @@ import warnings
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = '/root/reference'
+REF = None   # the reference checkout, from --reference or PYNUFFT_REFERENCE
 
 
 def _import_reference():
+    import tempfile
     os.environ['PYTHONDONTWRITEBYTECODE'] = '1'
     sys.dont_write_bytecode = True
-    os.makedirs('/tmp/refpkg', exist_ok=True)
-    link = '/tmp/refpkg/pynufft'
+    pkgdir = os.path.join(tempfile.gettempdir(), 'refpkg')
+    os.makedirs(pkgdir, exist_ok=True)
+    link = os.path.join(pkgdir, 'pynufft')
+    if os.path.islink(link) and os.readlink(link) != REF:
+        os.unlink(link)
     if not os.path.islink(link):
         os.symlink(REF, link)
-    sys.path.insert(0, '/tmp/refpkg')
+    sys.path.insert(0, pkgdir)
     warnings.filterwarnings('ignore')
     import pynufft
     from pynufft.src._helper import helper
@@ -141,6 +149,18 @@ def make_radial_c1(pynufft):
     print('radial_c1')
 
 
+def make_cg_c1(pynufft):
+    """solve(y, 'cg', maxiter=20) on the 2D radial plan (Nd 256^2, Kd 512^2, Jd 6^2)."""
+    om = radial_c1_om()
+    A = pynufft.NUFFT()
+    A.plan(om, (256, 256), (512, 512), (6, 6))
+    y = cplx(np.random.default_rng(100), (om.shape[0],))
+    x = A.solve(y, 'cg', maxiter=20)
+    np.savez_compressed(os.path.join(HERE, 'cg_c1.npz'), maxiter=20, y_seed=100,
+                        x=np.asarray(x, dtype=np.complex64))
+    print('cg_c1')
+
+
 def make_ndft_known_answer(pynufft):
     import scipy.io
     fhat = None
@@ -198,13 +218,25 @@ def make_l1tvols(pynufft):
 
 
 def main():
+    global REF
+    import argparse
+    ap = argparse.ArgumentParser(description=__doc__.split('\n')[0])
+    ap.add_argument('--reference', default=os.environ.get('PYNUFFT_REFERENCE'),
+                    help='path of the reference checkout (default: $PYNUFFT_REFERENCE)')
+    ap.add_argument('groups', nargs='*')
+    args = ap.parse_args()
+    if not args.reference or not os.path.isdir(args.reference):
+        ap.error('give the reference checkout with --reference or PYNUFFT_REFERENCE')
+    REF = os.path.abspath(args.reference)
     pynufft, helper = _import_reference()
-    only = sys.argv[1:]
+    only = args.groups
     if not only or 'plans' in only:
         for name, args in PLAN_CASES.items():
             make_plan_case(pynufft, helper, name, *args)
     if not only or 'radial' in only:
         make_radial_c1(pynufft)
+    if not only or 'cg' in only:
+        make_cg_c1(pynufft)
     if not only or 'ndft' in only:
         make_ndft_known_answer(pynufft)
     if not only or 'l1tvols' in only:

@@ -5,8 +5,8 @@ import numpy as np
 import pytest
 
 from conftest import PLAN_CASES, load_golden
-from oracle.nufft_oracle import (OracleNUFFT, alpha_beta_fit, interp_csr, minmax_T,
-                                 nudft_adjoint_pixels, nudft_forward_rows, rel_l2)
+from oracle.nufft_oracle import (ChunkedOracleNUFFT, OracleNUFFT, alpha_beta_fit, interp_csr,
+                                 minmax_T, nudft_adjoint_pixels, nudft_forward_rows, rel_l2)
 
 
 def _tup(a):
@@ -132,3 +132,51 @@ def test_oracle_l1tvols_matches_reference(tag):
     O.plan(g[f'om_{tag}'], Nd, Kd, Jd)
     x = O.l1tvols(g[f'y_{tag}'], int(g[f'maxiter_{tag}']), float(g[f'rho_{tag}']))
     assert rel_l2(x, g[f'x_{tag}']) < 1e-6
+
+
+def test_oracle_cg_c1_fixture():
+    """solve(y, 'cg', maxiter=20) on the 2D radial plan (256^2 / 512^2, J 6):
+    the oracle's restatement of scipy's CG against the reference's own
+    result (complex64 output, so ~1e-7 is rounding)."""
+    from tests_util import radial_c1_om
+    g = load_golden('cg_c1')
+    om = radial_c1_om()
+    O = OracleNUFFT()
+    O.plan(om, (256, 256), (512, 512), (6, 6))
+    y = _cplx(np.random.default_rng(int(g['y_seed'])), (om.shape[0],))
+    x, it = O.solve(y, 'cg', maxiter=int(g['maxiter']), return_info=True)
+    assert it == 20
+    assert rel_l2(x, g['x']) < 1e-6, rel_l2(x, g['x'])
+
+
+@pytest.mark.parametrize('batch', [None, 3])
+def test_chunked_oracle_equals_the_full_plan(batch):
+    """Planning on row chunks (forward concatenates, adjoint sums the chunks'
+    spH . y) gives the unchunked oracle's results bit for bit, and the
+    row-subset forward equals those rows of the full forward."""
+    rng = np.random.default_rng(6)
+    Nd, Kd, Jd = (10, 12, 8), (20, 24, 16), (6, 6, 6)
+    om = rng.uniform(-np.pi, np.pi, (2300, 3))
+    O = OracleNUFFT()
+    O.plan(om, Nd, Kd, Jd, batch=batch)
+    C = ChunkedOracleNUFFT()
+    C.plan(om, Nd, Kd, Jd, batch=batch, chunk=600)
+    tail = () if batch is None else (batch,)
+    x = _cplx(rng, Nd + tail)
+    y = _cplx(rng, (2300,) + tail)
+    assert np.array_equal(C.forward(x), O.forward(x))
+    assert np.array_equal(C.adjoint(y), O.adjoint(y))
+    rows = np.array([0, 599, 600, 1777, 2299])
+    assert np.array_equal(C.forward_rows(x, rows), O.forward(x)[rows])
+
+
+def test_nudft_adjoint_pixels_with_coils():
+    rng = np.random.default_rng(8)
+    Nd = (5, 6, 4)
+    om = rng.uniform(-np.pi, np.pi, (70, 3))
+    y = _cplx(rng, (70, 3))
+    pix = np.array([1, 50, 119])
+    got = nudft_adjoint_pixels(y, om, Nd, pix, chunk=16)
+    for b in range(3):
+        np.testing.assert_allclose(got[:, b], nudft_adjoint_pixels(y[:, b], om, Nd, pix),
+                                   rtol=1e-12, atol=1e-12)
