@@ -16,9 +16,20 @@ the device (CUDA events on the launching stream); `e2e` times the public API
 that the library records around every n-th of its launches (about 20 spread
 over the timed steps) on the launching stream;
 `cpu_baseline` times the CPU oracle (a restatement of the reference numpy
-path) on a bounded sample.  With --gpus N > 1 (torchrun) every rank runs an
+path: numpy FFT + scipy CSR products, one thread as in the reference) on one
+full forward+adjoint pair of the same workload after one warm-up pair;
+`batched` times the multi-coil workloads (2D golden-angle radial with 32
+coils; 3D kooshball with 8 coils in the deterministic gridding mode) against
+the same coils run one after another as single-coil transforms of the same
+points on the same GPU.  With --gpus N > 1 (torchrun) every rank runs an
 independent replica of the workload (no collective on the data path) and
 `value` is the sum over ranks.
+
+`--impl reference` times the oracle on the host for the same workload: the
+full plan, then --warmup untimed and --steps timed full forward+adjoint
+pairs, single-threaded like the reference's numpy/scipy calls (`value`),
+plus two pairs with the oracle's threaded products on every host core
+(`threaded`).
 """
 from __future__ import annotations
 
@@ -77,6 +88,41 @@ def workload(cfg: str):
         om = T.kooshball_3d(15625, 512)
         x = T.random_image(c['Nd'] + (8,), seed=0)
     return c, om, x
+
+
+def n_points(om):
+    return sum(o.shape[0] for o in om) if isinstance(om, list) else om.shape[0]
+
+
+def step_bytes(c, M):
+    """Per-point tables + samples + grid + image of one step (device working set)."""
+    B = c['batch'] or 1
+    ninst = c.get('ninst', 1)
+    return M * (8 * sum(c['Jd']) + 4 * len(c['Nd'])) + \
+        8 * (M + ninst * (int(np.prod(c['Kd'])) + int(np.prod(c['Nd'])))) * B
+
+
+def bench_config(cfg, world=1):
+    """The `config` object of the JSON line, identical in both arms."""
+    c = CONFIGS[cfg]
+    M = CONFIG_POINTS[cfg]
+    if M is None:
+        M = n_points(workload(cfg)[1])
+    B = c['batch'] or 1
+    ninst = c.get('ninst', 1)
+    ws = step_bytes(c, M)
+    if ws < L2_BYTES:
+        l2 = 'L2 flushed between timed steps (%d MB written; step data %.0f MB)' % (
+            FLUSH_BYTES >> 20, ws / 1e6)
+    else:
+        l2 = 'inputs larger than L2 (per-point tables %.0f MB + grid %.0f MB)' % (
+            M * (8 * sum(c['Jd']) + 4 * len(c['Nd'])) / 1e6,
+            8 * np.prod(c['Kd']) * B * ninst / 1e6)
+    return {'workload': c['name'], 'parallelism': f'replicas x{world}', 'l2': l2}
+
+
+CONFIG_POINTS = {'c1': 256 * 512, 'c2': 2_000_000, 'c3': 400 * 640, 'c4': 32 * 2048,
+                 'c5': 15625 * 512, 'c3i': None}
 
 
 def alg_bytes(c, M):
@@ -156,42 +202,49 @@ class ClockSampler:
                 'samples': len(sm), 'reasons': sorted(reasons)}
 
 
-def cpu_baseline(cfg, c, om, x, threads=1, steps=1, warmup=0, sample_points=100_000):
+def cpu_pairs(c, om, x, steps, warmup, threads=1, build_threads=None):
     """Time the CPU oracle (numpy FFT + scipy CSR, the reference's algorithm)
-    on a bounded sample: the FFT stages on the full grid, the sparse stages on
-    `sample_points` points, scaled linearly to the full M."""
+    on the full workload: plan once (CSR built with `build_threads`), then
+    `warmup` untimed and `steps` timed forward+adjoint pairs with `threads`
+    host threads.  Returns (seconds of each timed pair, plan seconds, oracle)."""
     from oracle.nufft_oracle import OracleNUFFT
-    M = om.shape[0]
-    ms = min(M, sample_points)
-    rng = np.random.default_rng(123)
-    sel = np.sort(rng.choice(M, ms, replace=False)) if ms < M else np.arange(M)
     O = OracleNUFFT()
     t0 = time.perf_counter()
-    O.plan(om[sel], c['Nd'], c['Kd'], c['Jd'], batch=c['batch'], threads=threads)
+    O.plan(om, c['Nd'], c['Kd'], c['Jd'], batch=c['batch'], threads=threads,
+           build_threads=build_threads or threads)
     t_plan = time.perf_counter() - t0
-    scale = M / ms
     times = []
     for it in range(warmup + steps):
         t0 = time.perf_counter()
-        k = O.xx2k(O.x2xx(x))
-        t1 = time.perf_counter()
-        y = O.k2y(k)
-        t2 = time.perf_counter()
-        kk = O.y2k(y)
-        t3 = time.perf_counter()
-        O.xx2x(O.k2xx(kk))
-        t4 = time.perf_counter()
+        O.adjoint(O.forward(x))
         if it >= warmup:
-            times.append((t1 - t0) + (t4 - t3) + scale * ((t2 - t1) + (t3 - t2)))
-    t_pair = float(np.median(times))
-    sample = (f'{ms} of {M} points ({ms / M:.1%}); FFT/scale stages on the full grid, '
-              f'sparse k2y/y2k timed on the sample and scaled x{scale:.1f}; plan {t_plan:.1f} s')
-    return 1.0 / t_pair, sample, t_pair
+            times.append(time.perf_counter() - t0)
+    return times, t_plan, O
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(cfg, c, om, x):
+    """One full pair of the workload on one host thread after one warm-up pair
+    (the reference's numpy FFT and scipy CSR products are single-threaded);
+    the CSR is built with every host core to keep the plan short."""
+    cores = host_cores()
+    times, t_plan, _ = cpu_pairs(c, om, x, steps=1, warmup=1, threads=1, build_threads=cores)
+    M = n_points(om)
+    sample = (f'1 full forward+adjoint pair (M={M}, all points) after 1 warm-up pair, 1 thread; '
+              f'plan {t_plan:.1f} s (CSR built on {cores} threads)')
+    return {'value': 1.0 / times[0], 'unit': 'pairs/s', 'cores': 1, 'kind': 'port',
+            'sample': sample}
 
 
 def run_reference(args, cfg, rank):
     """--impl reference: the CPU oracle (restating the reference numpy NUFFT)
-    with all host threads, same metric/unit, each step a bounded sample."""
+    on the same workload, every step a full forward+adjoint pair."""
     if rank != 0:
         return
     c, om, x = workload(cfg)
@@ -199,20 +252,123 @@ def run_reference(args, cfg, rank):
         print(json.dumps({'impl': 'reference', 'unavailable': 'the CPU reference arm times '
                           'single-instance configurations only'}), flush=True)
         return
-    threads = os.cpu_count() or 1
-    v, sample, t_pair = cpu_baseline(cfg, c, om, x, threads=threads, steps=args.steps,
-                                     warmup=args.warmup)
+    cores = host_cores()
+    t_start = time.perf_counter()
+    times, t_plan, O = cpu_pairs(c, om, x, steps=args.steps, warmup=args.warmup, threads=1,
+                                 build_threads=cores)
+    total = float(np.sum(times))
+    value = args.steps / total
+    # the same oracle with its row-chunked sparse products and FFTs on every core
+    O.threads = cores
+    O._row_chunks = None
+    tt = []
+    for it in range(3):
+        t0 = time.perf_counter()
+        O.adjoint(O.forward(x))
+        if it > 0:
+            tt.append(time.perf_counter() - t0)
+    M = n_points(om)
+    sample = (f'full workload (M={M}): plan {t_plan:.1f} s (CSR built on {cores} threads), '
+              f'{args.warmup} warm-up + {args.steps} timed forward+adjoint pairs on 1 thread '
+              f'(numpy FFT and scipy CSR products, single-threaded as in the reference)')
     line = {
-        'impl': 'reference', 'metric': 'NUFFT fwd+adj pairs/s', 'value': v, 'unit': 'pairs/s',
+        'impl': 'reference', 'metric': 'NUFFT fwd+adj pairs/s', 'value': value, 'unit': 'pairs/s',
         'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': 1e3 * t_pair, 'higher_is_better': True, 'scaling': 'weak',
+        'ms_per_step': 1e3 * total / args.steps, 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'c64 FFT / c128 CSR', 'data': 'synthetic',
-        'config': {'workload': c['name'], 'l2': 'host run'},
-        'cpu_baseline': {'value': v, 'unit': 'pairs/s', 'cores': threads, 'kind': 'port',
+        'config': bench_config(cfg, args.gpus),
+        'cpu_baseline': {'value': value, 'unit': 'pairs/s', 'cores': 1, 'kind': 'port',
                          'sample': sample},
-        'e2e': {'value': v, 'unit': 'pairs/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        'threaded': {'value': len(tt) / float(np.sum(tt)), 'unit': 'pairs/s', 'cores': cores,
+                     'sample': f'{len(tt)} pairs after 1 warm-up, the oracle\'s row-chunked CSR '
+                               f'products and scipy.fft on {cores} threads'},
+        'e2e': {'value': value, 'unit': 'pairs/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        'wall_s': time.perf_counter() - t_start,
     }
     print(json.dumps(line), flush=True)
+
+
+def time_pairs(torch, stream, fn, steps, warmup=3):
+    """Milliseconds per call of fn over `steps` calls after `warmup`, CUDA
+    events on the launching stream."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(steps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def batched_leg(torch, dev, peak, steps):
+    """Multi-coil workloads: coil-pairs/s of one batched plan against the
+    same coils run one after another through a single-coil plan of the same
+    points (the plain single-instance path) on the same GPU, and the batched
+    gridding / interpolation kernels against the HBM roofline."""
+    from ctypes import byref, c_double, c_int, c_void_p
+    from pynufft_gb300 import NUFFT
+    out = {}
+    stream = torch.cuda.current_stream(dev)
+    sp = c_void_p(stream.cuda_stream)
+    for cfg, det in (('c3', False), ('c5', True)):
+        c, om, x = workload(cfg)
+        B, M = c['batch'], om.shape[0]
+        A = NUFFT(dev)
+        A.plan(om, c['Nd'], c['Kd'], c['Jd'], batch=B, deterministic=det)
+        lib = A._lib
+        xd = torch.from_numpy(x).to(dev)
+        yd = torch.empty((M, B), dtype=torch.complex64, device=dev)
+        xo = torch.empty_like(xd)
+
+        def pair():
+            lib.nufft_forward(A._plan, c_void_p(xd.data_ptr()), c_void_p(yd.data_ptr()), sp)
+            lib.nufft_adjoint(A._plan, c_void_p(yd.data_ptr()), c_void_p(xo.data_ptr()), sp)
+        ms_b = time_pairs(torch, stream, pair, steps)
+        lib.nufft_plan_kernel_timing(A._plan, 1)
+        time_pairs(torch, stream, pair, max(3, steps // 2), warmup=0)
+        k_ms, y_ms, k_n, y_n = c_double(), c_double(), c_int(), c_int()
+        lib.nufft_plan_kernel_times(A._plan, byref(k_ms), byref(k_n), byref(y_ms), byref(y_n))
+        lib.nufft_plan_kernel_timing(A._plan, 0)
+        t_k2y = k_ms.value / max(k_n.value, 1)
+        t_y2k = y_ms.value / max(y_n.value, 1)
+        A.release()
+        del yd, xo
+        # the plain path: one single-coil plan, the coils' pairs one after another
+        P = NUFFT(dev)
+        P.plan(om, c['Nd'], c['Kd'], c['Jd'], deterministic=det)
+        xs = [xd[..., b].contiguous() for b in range(B)]
+        ys = [torch.empty((M,), dtype=torch.complex64, device=dev) for _ in range(B)]
+        xos = [torch.empty_like(xs[0]) for _ in range(B)]
+        del xd
+
+        def plain():
+            for b in range(B):
+                P._lib.nufft_forward(P._plan, c_void_p(xs[b].data_ptr()), c_void_p(ys[b].data_ptr()), sp)
+                P._lib.nufft_adjoint(P._plan, c_void_p(ys[b].data_ptr()), c_void_p(xos[b].data_ptr()), sp)
+        ms_p = time_pairs(torch, stream, plain, steps)
+        P.release()
+        del xs, ys, xos
+        torch.cuda.empty_cache()
+        nbytes = alg_bytes(c, M)
+        out[cfg] = {
+            'workload': c['name'] + (', deterministic gridding' if det else ''),
+            'coil_pairs_per_s': B * 1e3 / ms_b, 'ms_per_pair': ms_b,
+            'gridding': {'kernel': 'y2k', 'ms': t_y2k, 'gbs': nbytes / (t_y2k / 1e3) / 1e9,
+                         'frac': nbytes / (t_y2k / 1e3) / 1e9 / peak},
+            'interp': {'kernel': 'k2y', 'ms': t_k2y, 'gbs': nbytes / (t_k2y / 1e3) / 1e9,
+                       'frac': nbytes / (t_k2y / 1e3) / 1e9 / peak},
+            'alg_bytes': nbytes,
+            'plain': {'coil_pairs_per_s': B * 1e3 / ms_p, 'ms_per_coil_pair': ms_p / B,
+                      'how': f'{B} single-coil forward+adjoint pairs in turn through one '
+                             'single-coil plan of the same points'},
+            'speedup_vs_plain': ms_p / ms_b,
+            'steps': steps,
+        }
+    return out
 
 
 def main():
@@ -223,6 +379,9 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--config', default='c2', choices=sorted(CONFIGS))
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
+    ap.add_argument('--no-batched', action='store_true', help='skip the multi-coil leg')
+    ap.add_argument('--batched-steps', type=int, default=10,
+                    help='timed pairs per measurement of the multi-coil leg')
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -271,7 +430,7 @@ def main():
         lib.nufft_adjoint(A._plan, c_void_p(yd.data_ptr()), c_void_p(xo.data_ptr()), sp)
 
     # working set of one step: per-point tables + samples + grid + image
-    ws_bytes = M * (8 * sum(c['Jd']) + 4 * len(c['Nd'])) + 8 * (M + ninst * (np.prod(c['Kd']) + np.prod(c['Nd']))) * (c['batch'] or 1)
+    ws_bytes = step_bytes(c, M)
     flush = ws_bytes < L2_BYTES
     scratch = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device=dev) if flush else None
 
@@ -407,10 +566,18 @@ def main():
     h2d = (xh.numel() + yh.numel()) * 8
     d2h = (yh.numel() + xr.numel()) * 8
 
+    batched = None
+    if not args.no_batched and args.config == 'c2':
+        A.release()
+        del xd, yd, xo, xh, yh, xr
+        if scratch is not None:
+            del scratch
+        torch.cuda.empty_cache()
+        batched = batched_leg(torch, dev, peak, args.batched_steps)
+
     cpu = None
     if rank == 0 and not args.no_cpu and ninst == 1:
-        v, sample, _ = cpu_baseline(args.config, c, om, x, threads=1)
-        cpu = {'value': v, 'unit': 'pairs/s', 'cores': 1, 'kind': 'port', 'sample': sample}
+        cpu = cpu_baseline(args.config, c, om, x)
 
     if rank == 0:
         line = {
@@ -418,12 +585,7 @@ def main():
             'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
             'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'c64', 'data': 'synthetic',
-            'config': {'workload': c['name'], 'parallelism': f'replicas x{world}',
-                       'l2': (('L2 flushed between timed steps (%d MB written; step data %.0f MB)'
-                               % (FLUSH_BYTES >> 20, ws_bytes / 1e6)) if flush else
-                              'inputs larger than L2 (per-point tables %.0f MB + grid %.0f MB)' % (
-                                  M * (8 * sum(c['Jd']) + 4 * len(c['Nd'])) / 1e6,
-                                  8 * np.prod(c['Kd']) * (c['batch'] or 1) * ninst / 1e6))},
+            'config': bench_config(args.config, world),
             'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': ach, 'peak': peak,
                          'unit': 'GB/s', 'frac': ach / peak, 'peak_kind': peak_kind,
                          'traffic': traffic, 'alg_bytes': nbytes, 'ms': t_dom,
@@ -438,6 +600,7 @@ def main():
             'gpu_launches': launches_per_step * args.steps,
             'plan_ms': plan_ms,
             'cg': cg,
+            'batched': batched,
             'clocks': clk,
         }
         print(json.dumps(line), flush=True)
