@@ -389,9 +389,29 @@ class NUFFT:
     def k2y2k(self, k):
         return self._call(self._lib.nufft_k2y2k, k, 'k', 'k', 'k2y2k')
 
-    # the reference's *_one2one variants are the single-coil stages
-    xx2k_one2one = xx2k
-    k2xx_one2one = k2xx
+    # ---- single-image FFT stages (nufft/_nufft_class_methods_cpu.py:251-264, 332-344)
+    def _single_image_plan(self):
+        """This plan when it is one coil and one instance; otherwise a
+        point-free single-coil plan of the same Nd/Kd/Jd (kept), whose FFT
+        stages transform one Nd image."""
+        if self.B == 1 and self.ninst == 1:
+            return self
+        one = getattr(self, '_one2one', None)
+        if one is None or one.Nd != self.Nd or one.Kd != self.Kd or one.Jd != self.Jd:
+            one = NUFFT(self.device)
+            one.plan(numpy.zeros((0, self.ndims)), self.Nd, self.Kd, self.Jd)
+            self._one2one = one
+        return one
+
+    def xx2k_one2one(self, xx):
+        """Zero-pad one Nd image into Kd and FFT it (no scaling), whatever the
+        plan's batch: Nd -> Kd (nufft/__init__.py:722-724)."""
+        return self._single_image_plan().xx2k(xx)
+
+    def k2xx_one2one(self, k):
+        """Inverse FFT of one Kd spectrum and crop to Nd (no scaling): Kd ->
+        Nd (nufft/__init__.py:718-720)."""
+        return self._single_image_plan().k2xx(k)
 
     # ---- SENSE coil operators (deprecated reference class, linalg/nufft_cpu.py:163-203)
     def set_sense(self, coil_profile):
@@ -494,8 +514,9 @@ class NUFFT:
         """solve(y, 'cg', maxiter=...) (linalg/solve_cpu.py:256-288 via
         nufft/_nufft_class_methods_cpu.py:150-166): CG on the k-space normal
         operator, x0 = 0, scipy's rtol/atol stopping rule, then k2xx(k)/sn.
-        'L1TVOLS' runs in the library (nufft_solve_l1tvols); 'dc', 'lsqr' and
-        'lsmr' are in ``pynufft_gb300.solvers``."""
+        'L1TVOLS' runs in the library (nufft_solve_l1tvols); 'dc', 'lsqr',
+        'lsmr', 'bicg', 'bicgstab', 'gmres' and 'lgmres' are in
+        ``pynufft_gb300.solvers``."""
         if solver is None:
             raise ValueError('solver must be given, e.g. solve(y, "cg", maxiter=20)')
         if solver == 'L1TVOLS':
