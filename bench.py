@@ -382,6 +382,8 @@ def main():
     ap.add_argument('--no-batched', action='store_true', help='skip the multi-coil leg')
     ap.add_argument('--batched-steps', type=int, default=10,
                     help='timed pairs per measurement of the multi-coil leg')
+    ap.add_argument('--batched-only', action='store_true',
+                    help='print only the multi-coil leg (a development aid; not a bench line)')
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -399,9 +401,13 @@ def main():
         import torch.distributed as dist
         dist.init_process_group('nccl', device_id=torch.device('cuda', local))
 
+    dev = torch.device('cuda', local)
+    if args.batched_only:
+        print(json.dumps({'batched': batched_leg(torch, dev, peaks()[0], args.batched_steps)}),
+              flush=True)
+        return
     from pynufft_gb300 import NUFFT, _lib
     c, om, x = workload(args.config)
-    dev = torch.device('cuda', local)
     A = NUFFT(dev)
     ninst = c.get('ninst', 1)
 

@@ -48,6 +48,12 @@ nufft::Geom nufft_plan_s::geom() const {
     g.kerr = d_kerr;
     g.sub = d_sub;
     g.nsub = nsub;
+    g.maxsub = maxsub;
+    g.gsub = d_gsub;
+    g.ngsub = ngsub;
+    g.rsub = d_rsub;
+    g.nrsub = nrsub;
+    g.rgroup = rgroup;
     // lane mappings: coil-teams for B >= 8; otherwise the plan's choice.  The
     // defaults (fastest in measurement on 2D radial and 3D uniform
     // trajectories; the autotuner may pick others): k2y gathers from a shared
@@ -445,6 +451,10 @@ int nufft_adjoint(nufft_plan_t p, const void* y, void* x, void* stream) {
         NUFFT_CUDA_TRY(cudaEventRecord(p->ev_adj, s));
         p->adj_used = true;
         return st;
+    }
+    if (cm_path(p)) {   // several coils: the gridded spectra are written coil-major
+        NUFFT_TRY(launch_y2k_cm(p, (const float2*)y, p->d_cm, s));
+        return cm_to_image(p, (float2*)x, true, false, s);
     }
     NUFFT_TRY(launch_y2k(p, (const float2*)y, p->d_grid, s));
     if (p->B > 1) return image_from_spectrum_coils(p, p->d_grid, (float2*)x, true, false, s);

@@ -439,13 +439,10 @@ static int fft_cm_exec(nufft_plan_s* p, int direction, cudaStream_t s) {
     return NUFFT_OK;
 }
 
-// Several coils: spectrum k (coil-fastest) -> image xx (coil-fastest):
-// transpose to coil-major, inverse FFTs there, crop straight from the
-// coil-major spectra (x sn when apply_sn, / sn when divide_sn).  k is read
-// only.
-int image_from_spectrum_coils(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn,
-                              bool divide_sn, cudaStream_t s) {
-    NUFFT_TRY(coil_transpose(p, k, p->d_cm, true, s));
+// Several coils: the coil-major spectra in p->d_cm -> image xx (coil-fastest):
+// inverse FFTs in place, then the crop straight from the coil-major spectra
+// (x sn when apply_sn, / sn when divide_sn, / prod(Kd)).
+int cm_to_image(nufft_plan_s* p, float2* xx, bool apply_sn, bool divide_sn, cudaStream_t s) {
     NUFFT_TRY(fft_cm_exec(p, +1, s));
     ImgGeom g = img_geom(p);
     const float norm = (float)(1.0 / (double)p->prodK);
@@ -461,6 +458,32 @@ int image_from_spectrum_coils(nufft_plan_s* p, const float2* k, float2* xx, bool
     return check_launch("crop_cm_rows_kernel");
 }
 
+// Several coils: spectrum k (coil-fastest) -> image xx (coil-fastest):
+// transpose to coil-major, then cm_to_image.  k is read only.
+int image_from_spectrum_coils(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn,
+                              bool divide_sn, cudaStream_t s) {
+    NUFFT_TRY(coil_transpose(p, k, p->d_cm, true, s));
+    return cm_to_image(p, xx, apply_sn, divide_sn, s);
+}
+
+// Several coils: image xx (coil-fastest) -> coil-major spectra in p->d_cm:
+// every coil's grid padded straight into the coil-major buffer (x sn when
+// apply_sn), then the forward FFTs in place.
+int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s) {
+    ImgGeom g = img_geom(p);
+    const int64_t rows = rows_of(g, g.K, p->ninst);
+    const unsigned nb = row_blocks(p, rows);
+    const int nt = row_threads(g.K[g.ndim - 1] * g.B);
+    const int as = apply_sn ? 1 : 0;
+    switch (p->ndim) {
+        case 1: pad_cm_rows_kernel<1><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, rows); break;
+        case 2: pad_cm_rows_kernel<2><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, rows); break;
+        default: pad_cm_rows_kernel<3><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, rows); break;
+    }
+    NUFFT_TRY(check_launch("pad_cm_rows_kernel"));
+    return fft_cm_exec(p, -1, s);
+}
+
 // Image (Nd, caller's layout) -> oversampled spectrum k: zero-pad (x sn when
 // apply_sn) and forward FFT.  For one coil and one instance the pad only
 // writes the Nd corner of the plan's padded input buffer (its zeros are
@@ -472,18 +495,7 @@ int forward_from_image(nufft_plan_s* p, const float2* xx, bool apply_sn, float2*
                        cudaStream_t s) {
     if (p->B > 1) {
         // coil-major: pad every coil's grid, transform there, transpose to k
-        ImgGeom g = img_geom(p);
-        const int64_t rows = rows_of(g, g.K, p->ninst);
-        const unsigned nb = row_blocks(p, rows);
-        const int nt = row_threads(g.K[g.ndim - 1] * g.B);
-        const int as = apply_sn ? 1 : 0;
-        switch (p->ndim) {
-            case 1: pad_cm_rows_kernel<1><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, rows); break;
-            case 2: pad_cm_rows_kernel<2><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, rows); break;
-            default: pad_cm_rows_kernel<3><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, rows); break;
-        }
-        NUFFT_TRY(check_launch("pad_cm_rows_kernel"));
-        NUFFT_TRY(fft_cm_exec(p, -1, s));
+        NUFFT_TRY(image_to_cm(p, xx, apply_sn, s));
         return coil_transpose(p, p->d_cm, k, false, s);
     }
     if (p->pfft) return pfft_forward(p, xx, apply_sn, k, s);

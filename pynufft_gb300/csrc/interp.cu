@@ -2,6 +2,7 @@
 // fixed-point helpers of the deterministic gridding mode.  The kernel
 // instantiations live in interp_d1.cu / interp_d2.cu / interp_d3.cu.
 #include "nufft_internal.cuh"
+#include "interp_cm.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -17,6 +18,12 @@ int y2k_dim2(int jm, bool det, const Geom& g, const float2* y, float2* grid,
              unsigned long long* igrid, const double* dscal, cudaStream_t s);
 int y2k_dim3(int jm, bool det, const Geom& g, const float2* y, float2* grid,
              unsigned long long* igrid, const double* dscal, cudaStream_t s);
+int k2y_cm_dim2(int jm, const Geom& g, const float2* grid, float2* y, cudaStream_t s);
+int k2y_cm_dim3(int jm, const Geom& g, const float2* grid, float2* y, cudaStream_t s);
+int y2k_cm_dim2(int jm, bool det, const Geom& g, const float2* y, float2* grid,
+                unsigned long long* igrid, const double* dscal, cudaStream_t s);
+int y2k_cm_dim3(int jm, bool det, const Geom& g, const float2* y, float2* grid,
+                unsigned long long* igrid, const double* dscal, cudaStream_t s);
 
 static int pick_jm(const nufft_plan_s* p) {
     int j = 1;
@@ -160,26 +167,104 @@ int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s, b
     // deterministic: exact fixed-point accumulation, then one rounding to float
     if (!p->d_igrid) {
         NUFFT_CUDA_TRY(cudaMalloc(&p->d_igrid, sizeof(unsigned long long) * 2 * ncells));
-        NUFFT_CUDA_TRY(cudaMalloc(&p->d_dscal, sizeof(double) * (2 + 1024)));
-        p->dev_bytes += sizeof(unsigned long long) * 2 * ncells + sizeof(double) * 1026;
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_dscal, sizeof(double) * kScaleSlots));
+        p->dev_bytes += sizeof(unsigned long long) * 2 * ncells + sizeof(double) * kScaleSlots;
     }
     NUFFT_CUDA_TRY(cudaMemsetAsync(p->d_igrid, 0, sizeof(unsigned long long) * 2 * ncells, s));
     const int64_t ny = p->M * (int64_t)p->B;
-    const int nparts = 1024;
+    const int nparts = kAbsSumParts;
     double* part = p->d_dscal + 2;
     abs_sum_partial_kernel<<<nparts, 256, 0, s>>>(y, ny, part);
     NUFFT_TRY(check_launch("abs_sum_partial_kernel"));
     fixed_scale_kernel<<<1, 256, 0, s>>>(part, nparts, p->wmax, p->d_dscal);
     NUFFT_TRY(check_launch("fixed_scale_kernel"));
-    if (p->M > 0) NUFFT_TRY(y2k_dim<true>(p, g, y, nullptr, p->d_igrid, p->d_dscal, s));
+    if (p->M > 0) {
+        const bool timed = kernel_time_start(p, 1, s);
+        const int st = y2k_dim<true>(p, g, y, nullptr, p->d_igrid, p->d_dscal, s);
+        kernel_time_stop(p, 1, s, timed);
+        NUFFT_TRY(st);
+    }
     const int blocks = (int)std::min<size_t>((ncells + 255) / 256, (size_t)p->num_sms * 16);
     fixed_to_float_kernel<<<std::max(blocks, 1), 256, 0, s>>>(p->d_igrid, (int64_t)ncells,
                                                                p->d_dscal, grid);
     return check_launch("fixed_to_float_kernel");
 }
 
+// ---------------------------------------------------------------------------
+// coil-major spectra (plans of 8 or more coils)
+// ---------------------------------------------------------------------------
+// The row kernels are built for J in {4, 6, 8} on every axis, B a multiple
+// of 8, and the default bins of such plans (innermost extent 16 in 2D, 8 in
+// 3D); tiles must not wrap onto themselves and the gather's tile of at least
+// four coils must fit in shared memory.
+bool cm_path(const nufft_plan_s* p) {
+    if (p->B < 8 || p->B % 8 != 0 || (p->ndim != 2 && p->ndim != 3) || !p->d_cm || !p->d_rsub)
+        return false;
+    const int J = p->Jd[0];
+    if (J != 4 && J != 6 && J != 8) return false;
+    const int DI = p->ndim - 1;
+    for (int d = 0; d < p->ndim; ++d) {
+        if (p->Jd[d] != J) return false;
+        if (p->bs[d] + J - 1 > p->Kd[d]) return false;
+    }
+    // rows of 16 cells (bins x group along the innermost axis), not wrapping onto themselves
+    if (p->bs[DI] * p->rgroup != 16 || 16 + J - 1 > p->Kd[DI]) return false;
+    const int nkey = p->bs[0] * (p->ndim == 3 ? p->bs[1] : 1);
+    return nkey <= 256 && rows_smem(p->ndim, J, nkey, kRowSub, 8) <= 200 * 1024;
+}
+
+int launch_k2y_cm(nufft_plan_s* p, const float2* grid_cm, float2* y, cudaStream_t s) {
+    if (p->M == 0) return NUFFT_OK;
+    Geom g = p->geom();
+    const int jm = pick_jm(p);
+    const bool timed = kernel_time_start(p, 0, s);
+    const int st = (p->ndim == 2) ? k2y_cm_dim2(jm, g, grid_cm, y, s) : k2y_cm_dim3(jm, g, grid_cm, y, s);
+    kernel_time_stop(p, 0, s, timed);
+    return st;
+}
+
+int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s) {
+    const size_t ncells = (size_t)p->ninst * p->prodK * p->B;
+    Geom g = p->geom();
+    const int jm = pick_jm(p);
+    if (!(p->flags & NUFFT_FLAG_DETERMINISTIC)) {
+        NUFFT_CUDA_TRY(cudaMemsetAsync(grid_cm, 0, sizeof(float2) * ncells, s));
+        if (p->M == 0) return NUFFT_OK;
+        const bool timed = kernel_time_start(p, 1, s);
+        const int st = (p->ndim == 2) ? y2k_cm_dim2(jm, false, g, y, grid_cm, nullptr, nullptr, s)
+                                      : y2k_cm_dim3(jm, false, g, y, grid_cm, nullptr, nullptr, s);
+        kernel_time_stop(p, 1, s, timed);
+        return st;
+    }
+    // deterministic: per-row float sums in a fixed order, combined across
+    // tiles exactly in 64-bit fixed point, then one rounding to float
+    if (!p->d_igrid) {
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_igrid, sizeof(unsigned long long) * 2 * ncells));
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_dscal, sizeof(double) * kScaleSlots));
+        p->dev_bytes += sizeof(unsigned long long) * 2 * ncells + sizeof(double) * kScaleSlots;
+    }
+    NUFFT_CUDA_TRY(cudaMemsetAsync(p->d_igrid, 0, sizeof(unsigned long long) * 2 * ncells, s));
+    const int64_t ny = p->M * (int64_t)p->B;
+    abs_sum_partial_kernel<<<kAbsSumParts, 256, 0, s>>>(y, ny, p->d_dscal + 2);
+    NUFFT_TRY(check_launch("abs_sum_partial_kernel"));
+    fixed_scale_kernel<<<1, 256, 0, s>>>(p->d_dscal + 2, kAbsSumParts, p->wmax, p->d_dscal);
+    NUFFT_TRY(check_launch("fixed_scale_kernel"));
+    if (p->M > 0) {
+        const bool timed = kernel_time_start(p, 1, s);
+        const int st = (p->ndim == 2)
+                           ? y2k_cm_dim2(jm, true, g, y, nullptr, p->d_igrid, p->d_dscal, s)
+                           : y2k_cm_dim3(jm, true, g, y, nullptr, p->d_igrid, p->d_dscal, s);
+        kernel_time_stop(p, 1, s, timed);
+        NUFFT_TRY(st);
+    }
+    const int blocks = (int)std::min<size_t>((ncells + 255) / 256, (size_t)p->num_sms * 16);
+    fixed_to_float_kernel<<<std::max(blocks, 1), 256, 0, s>>>(p->d_igrid, (int64_t)ncells,
+                                                               p->d_dscal, grid_cm);
+    return check_launch("fixed_to_float_kernel");
+}
+
 // Exact (fixed-point) gridding into `grid` using caller-provided scratch:
-// acc holds 2 * ninst * prodK * B accumulators, scal 2 + 1024 doubles.
+// acc holds 2 * ninst * prodK * B accumulators, scal kScaleSlots doubles.
 // Allocates nothing.
 int launch_y2k_exact_into(const nufft_plan_s* p, const float2* y, float2* grid,
                           unsigned long long* acc, double* scal, cudaStream_t s) {
@@ -188,7 +273,7 @@ int launch_y2k_exact_into(const nufft_plan_s* p, const float2* y, float2* grid,
     g.ymethod = (p->B >= 8) ? NUFFT_Y2K_COIL : NUFFT_Y2K_ZTEAM;
     NUFFT_CUDA_TRY(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * 2 * ncells, s));
     const int64_t ny = p->M * (int64_t)p->B;
-    const int nparts = 1024;
+    const int nparts = kAbsSumParts;
     abs_sum_partial_kernel<<<nparts, 256, 0, s>>>(y, ny, scal + 2);
     NUFFT_TRY(check_launch("abs_sum_partial_kernel"));
     fixed_scale_kernel<<<1, 256, 0, s>>>(scal + 2, nparts, p->wmax, scal);

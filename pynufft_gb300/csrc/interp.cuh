@@ -693,7 +693,8 @@ __global__ void __launch_bounds__(512) k2y_ctile_kernel(Geom g, const float2* __
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t s_bar;
     float2* tile = reinterpret_cast<float2*>(smem_raw);
-    const int4 sp = g.sub[blockIdx.x];
+    // the gather list (bins split only past kGatherSub points) when the plan has one
+    const int4 sp = (g.gsub ? g.gsub : g.sub)[blockIdx.x];
     int o[3];
     tile_origin<DIM>(g, sp, o);
     constexpr int DI = DIM - 1;

@@ -1,0 +1,376 @@
+// Coil-major interpolation and gridding for plans of 8 or more coils.
+//
+// The forward and adjoint transforms of a multi-coil plan keep the
+// oversampled spectra coil-major -- grid_cm[(inst * B + b) * prod(Kd) + cell]
+// -- from the FFTs through the interpolation / gridding, so the spectra need
+// no coil-fastest copy.  (The reference's batch layout, coil fastest in
+// x / k / y, linalg/nufft_hsa.py:203-228, is kept at the API: images and
+// samples stay coil-fastest; only the internal spectra are coil-major.)
+//
+// Gridding (y2k_rows_kernel).  A block takes one sub-problem (a chunk of one
+// bin's points) and the tile (bin + J-1 halo) it scatters to.  The tile is
+// cut into "rows" along the innermost axis (Tz cells each); a warp holds the
+// sums of RS rows x CB coils in registers (lane = row slot x coil, TZ
+// complex accumulators per lane) and visits, in a fixed order, every point
+// whose footprint crosses those rows: u = y conj(c_x c_y) for its row, then
+// the J innermost taps acc[pz + k] += u conj(c_z[k]) at register indices
+// chosen by a warp-uniform switch on pz.  No shared-memory atomics and no
+// float-to-integer conversions per tap; the rows' sums are flushed once per
+// row block through a per-warp shared transpose, so each (row, coil) goes
+// out as a contiguous run of Tz cells: float2 atomics into the grid (fast
+// mode), or 64-bit fixed-point integer atomics (deterministic mode: the
+// per-row float sums are a fixed-order reduction, their combination across
+// tiles is exact, so the result is bitwise reproducible).
+//
+// Interpolation (k2y_cmtile_kernel).  The block loads its sub-problem's tile
+// for a chunk of CBK coils from the coil-major grid into shared memory with
+// the coils fastest (each thread reads runs of four cells of one coil's row
+// and writes them coil-fastest), then teams of G lanes (one point each,
+// lanes over coils) gather the Kronecker sums from the tile.
+#pragma once
+#include "interp.cuh"
+
+namespace nufft {
+
+// Row slots of a warp: RS0 x RS1 (axis 0 x axis 1 rows) with RS0 * RS1 =
+// 32 / CB; 2D rows run along axis 1 and are indexed by axis 0 only.
+template <int DIM, int CB>
+struct RowSlots {
+    static constexpr int RS = 32 / CB;
+    static constexpr int RS0 = (DIM == 2) ? RS : ((RS == 4) ? 2 : 1);
+    static constexpr int RS1 = (DIM == 2) ? 1 : RS / RS0;
+};
+
+// acc[PZ + k] += u * conj(cz[k]), k < JM, at compile-time register indices.
+template <int PZ, int TZ, int JM>
+__device__ __forceinline__ void row_taps(float2 (&acc)[TZ], float2 u, const float2 (&cz)[JM]) {
+    if constexpr (PZ + JM <= TZ) {
+#pragma unroll
+        for (int k = 0; k < JM; ++k) {
+            acc[PZ + k].x = fmaf(u.x, cz[k].x, fmaf(u.y, cz[k].y, acc[PZ + k].x));
+            acc[PZ + k].y = fmaf(u.y, cz[k].x, fmaf(-u.x, cz[k].y, acc[PZ + k].y));
+        }
+    }
+}
+
+template <int TZ, int JM>
+__device__ __forceinline__ void row_taps_at(int pz, float2 (&acc)[TZ], float2 u,
+                                            const float2 (&cz)[JM]) {
+    static_assert(TZ - JM + 1 <= 32, "at most 32 tap offsets per row");
+    switch (pz) {
+#define NUFFT_ROW_CASE(c) \
+    case c: row_taps<c, TZ, JM>(acc, u, cz); break;
+        NUFFT_ROW_CASE(0) NUFFT_ROW_CASE(1) NUFFT_ROW_CASE(2) NUFFT_ROW_CASE(3)
+        NUFFT_ROW_CASE(4) NUFFT_ROW_CASE(5) NUFFT_ROW_CASE(6) NUFFT_ROW_CASE(7)
+        NUFFT_ROW_CASE(8) NUFFT_ROW_CASE(9) NUFFT_ROW_CASE(10) NUFFT_ROW_CASE(11)
+        NUFFT_ROW_CASE(12) NUFFT_ROW_CASE(13) NUFFT_ROW_CASE(14) NUFFT_ROW_CASE(15)
+        NUFFT_ROW_CASE(16) NUFFT_ROW_CASE(17) NUFFT_ROW_CASE(18) NUFFT_ROW_CASE(19)
+        NUFFT_ROW_CASE(20) NUFFT_ROW_CASE(21) NUFFT_ROW_CASE(22) NUFFT_ROW_CASE(23)
+        NUFFT_ROW_CASE(24) NUFFT_ROW_CASE(25) NUFFT_ROW_CASE(26) NUFFT_ROW_CASE(27)
+        NUFFT_ROW_CASE(28) NUFFT_ROW_CASE(29) NUFFT_ROW_CASE(30) NUFFT_ROW_CASE(31)
+#undef NUFFT_ROW_CASE
+        default: break;
+    }
+}
+
+// Counting sort of a sub-problem's points by row key (in-block):
+// list[off[k] ..] = the local indices i, ascending, of the points whose row
+// key is k.  key(i) must lie in [0, nkey).  Warp w ranks the contiguous run
+// of points [w * chunk, (w + 1) * chunk) in rounds of 32 with match-any
+// peer masks, so the order is fixed by the inputs alone.  Uses the per-warp
+// histogram wcnt[nwarps][nkey]; ends with a block barrier.
+template <typename KeyFn>
+__device__ void sort_rows(int P, int nkey, KeyFn key, int* __restrict__ wcnt,
+                          int* __restrict__ off, int* __restrict__ list) {
+    const int nwarps = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int chunk = ((P + nwarps - 1) / nwarps + 31) & ~31;
+    const int first = w * chunk, last = min(P, first + chunk);
+    for (int e = threadIdx.x; e < nwarps * nkey; e += blockDim.x) wcnt[e] = 0;
+    __syncthreads();
+    int* mine = wcnt + w * nkey;
+    // pass 1: points per (warp, key)
+    for (int base = first; base < last; base += 32) {
+        const int i = base + lane;
+        const int k = (i < last) ? key(i) : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, k);
+        if (k >= 0 && lane == __ffs(peers) - 1) mine[k] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // per key: exclusive prefixes over warps in place, totals into off[k + 1]
+    for (int k = threadIdx.x; k < nkey; k += blockDim.x) {
+        int run = 0;
+        for (int q = 0; q < nwarps; ++q) {
+            const int c = wcnt[q * nkey + k];
+            wcnt[q * nkey + k] = run;
+            run += c;
+        }
+        off[k + 1] = run;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        off[0] = 0;
+        for (int k = 0; k < nkey; ++k) off[k + 1] += off[k];
+    }
+    __syncthreads();
+    // pass 2: place each point after its warp's earlier points of that key
+    for (int base = first; base < last; base += 32) {
+        const int i = base + lane;
+        const int k = (i < last) ? key(i) : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, k);
+        if (k >= 0) list[off[k] + mine[k] + __popc(peers & ((1u << lane) - 1u))] = i;
+        __syncwarp();
+        if (k >= 0 && lane == __ffs(peers) - 1) mine[k] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+}
+
+// Shared memory of y2k_rows_kernel (bytes), for nkey row keys, at most P
+// points and a block of nwarps warps: the staged per-point data
+// (coefficients, packed tile offsets, sample index) and the row sort's
+// histogram, offsets and list.
+__host__ __device__ inline size_t rows_smem(int DIM, int JM, int nkey, int P, int nwarps) {
+    return sizeof(float2) * (size_t)P * DIM * JM +
+           sizeof(int) * ((size_t)2 * P + (size_t)nwarps * nkey + nkey + 1 + P) + 16;
+}
+
+// Row gridding.  One block per row sub-problem: up to g.rgroup consecutive
+// bins along the innermost axis (3D), at most kRowSub points; the tile is
+// (bs0 + J - 1) x (bs1 + J - 1) rows of TZ = rgroup * bs_z + J - 1 cells.
+template <int DIM, int JM, int TZ, int CB, bool DET>
+__global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __restrict__ y,
+                                                       float2* __restrict__ grid,
+                                                       unsigned long long* __restrict__ igrid,
+                                                       const double* __restrict__ dscal) {
+    static_assert(DIM == 2 || DIM == 3, "rows of a 2D or 3D tile");
+    using RSl = RowSlots<DIM, CB>;
+    constexpr int RS0 = RSl::RS0, RS1 = RSl::RS1;
+    constexpr int DI = DIM - 1;
+    constexpr int PC = DIM * JM; // staged coefficients per point
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int4 sp = g.rsub[blockIdx.x];
+    const int P = sp.z;
+    int o[3];
+    tile_origin<DIM>(g, sp, o);
+    const int bs0 = g.bs[0], bs1 = (DIM == 3) ? g.bs[1] : 1;
+    const int nkey = bs0 * bs1;
+    const int nwarps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float2* scoef = reinterpret_cast<float2*>(smem_raw);                 // kRowSub x DIM x JM
+    int* sinfo = reinterpret_cast<int*>(scoef + (size_t)kRowSub * PC);   // pz | lx << 8 | ly << 16
+    int* sm = sinfo + kRowSub;                                           // sample index
+    int* wcnt = sm + kRowSub;
+    int* off = wcnt + nwarps * nkey;
+    int* list = off + nkey + 1;
+
+    const int* __restrict__ pos0 = g.pos[0];
+    const int* __restrict__ pos1 = g.pos[DIM == 3 ? 1 : 0];
+    auto key = [&](int i) {
+        const int s = sp.y + i;
+        const int lx = __ldg(pos0 + s) - o[0];
+        if constexpr (DIM == 3) return lx * bs1 + (__ldg(pos1 + s) - o[1]);
+        return lx;
+    };
+    sort_rows(P, nkey, key, wcnt, off, list);
+    // stage the points in row order: coefficients, offsets in the tile, sample
+    for (int e = threadIdx.x; e < P * PC; e += blockDim.x) {
+        const int j = e / PC, r = e - j * PC, d = r / JM, k = r - d * JM;
+        const int s = sp.y + list[j];
+        scoef[e] = __ldg(g.coef[d] + (size_t)s * g.JP[d] + k);
+    }
+    for (int j = threadIdx.x; j < P; j += blockDim.x) {
+        const int s = sp.y + list[j];
+        const int lx = __ldg(pos0 + s) - o[0];
+        const int ly = (DIM == 3) ? __ldg(pos1 + s) - o[1] : 0;
+        const int pz = __ldg(g.pos[DI] + s) - o[DI];
+        sinfo[j] = pz | (lx << 8) | (ly << 16);
+        sm[j] = __ldg(g.perm + s);
+    }
+    __syncthreads();
+
+    const int B = g.B;
+    const int T0 = g.T[0], T1 = (DIM == 3) ? g.T[1] : 1;
+    const int nrb0 = (T0 + RS0 - 1) / RS0, nrb1 = (T1 + RS1 - 1) / RS1;
+    const int nrb = nrb0 * nrb1;
+    const int slot = lane / CB, b = lane % CB;
+    const int gx = slot / RS1, gy = slot % RS1;
+    const size_t ibase = (size_t)sp.w * B;
+    const float fscale = DET ? (float)dscal[1] : 1.f;
+    // a tile that does not wrap around the periodic grid addresses rows and
+    // cells without wrapping
+    bool interior = o[DI] + TZ <= g.K[DI];
+#pragma unroll
+    for (int d = 0; d < DIM - 1; ++d) interior = interior && (o[d] + g.T[d] <= g.K[d]);
+    const int Kz = g.K[DI];
+
+    for (int b0 = 0; b0 < B; b0 += CB) {
+        const float2* __restrict__ yc = y + b0 + b;
+        for (int rb = warp; rb < nrb; rb += nwarps) {
+            const int R0 = (rb / nrb1) * RS0, R1 = (rb % nrb1) * RS1;
+            float2 acc[TZ];
+#pragma unroll
+            for (int c = 0; c < TZ; ++c) acc[c] = make_float2(0.f, 0.f);
+            bool touched = false;
+            const int lx_lo = max(0, R0 - JM + 1), lx_hi = min(bs0 - 1, R0 + RS0 - 1);
+            const int ly_lo = max(0, R1 - JM + 1), ly_hi = min(bs1 - 1, R1 + RS1 - 1);
+            for (int lx = lx_lo; lx <= lx_hi; ++lx) {
+                const int kb = lx * bs1;
+                const int j0 = off[kb + ly_lo], j1 = off[kb + ly_hi + 1];
+                if (j0 >= j1) continue;
+                touched = true;
+                const int ix = R0 + gx - lx;
+                float2 ynext = __ldg(yc + (size_t)sm[j0] * B);
+                for (int j = j0; j < j1; ++j) {
+                    const float2 yv = ynext;
+                    if (j + 1 < j1) ynext = __ldg(yc + (size_t)sm[j + 1] * B);
+                    const int info = sinfo[j];
+                    const float2* cj = scoef + (size_t)j * PC;
+                    float2 w = make_float2(0.f, 0.f);
+                    if constexpr (DIM == 3) {
+                        const int iy = R1 + gy - (info >> 16);
+                        if (ix >= 0 && ix < JM && iy >= 0 && iy < JM) w = cmul(cj[ix], cj[JM + iy]);
+                    } else {
+                        if (ix >= 0 && ix < JM) w = cj[ix];
+                    }
+                    float2 cz[JM];
+#pragma unroll
+                    for (int k = 0; k < JM; ++k) cz[k] = cj[DI * JM + k];
+                    row_taps_at<TZ, JM>(info & 255, acc, cmulc(yv, w), cz);
+                }
+            }
+            if (!touched) continue;   // warp-uniform: no point crosses these rows
+            // flush each lane's row (row slot, coil) straight from registers
+            const int rx = R0 + gx, ry = R1 + gy;
+            if (rx >= T0 || ry >= T1) continue;
+            size_t row;
+            if constexpr (DIM == 3) {
+                const int X = interior ? o[0] + rx : wrapn(o[0] + rx, g.K[0]);
+                const int Y = interior ? o[1] + ry : wrapn(o[1] + ry, g.K[1]);
+                row = (size_t)X * g.K[1] + Y;
+            } else {
+                row = (size_t)(interior ? o[0] + rx : wrapn(o[0] + rx, g.K[0]));
+            }
+            // a row holds TZ <= Kz cells, so it wraps at most once: cells
+            // [0, cw) from o_z on, cells [cw, TZ) from 0
+            const size_t rbase = (ibase + b0 + b) * (size_t)g.prodK + row * Kz;
+            const int cw = interior ? TZ : Kz - o[DI];
+            const size_t e0 = rbase + o[DI];
+#pragma unroll
+            for (int c = 0; c < TZ; ++c) {
+                const float2 v = acc[c];
+                if (v.x == 0.f && v.y == 0.f) continue;
+                const size_t e = e0 + ((c < cw) ? c : c - Kz);   // wrapped past the row end
+                if constexpr (DET) {
+                    atomicAdd(igrid + 2 * e, (unsigned long long)__float2ll_rn(v.x * fscale));
+                    atomicAdd(igrid + 2 * e + 1, (unsigned long long)__float2ll_rn(v.y * fscale));
+                } else {
+                    atomicAdd(grid + e, v);
+                }
+            }
+        }
+    }
+}
+
+// Shared memory of k2y_cmtile_kernel (bytes): the tile of CBK coils, each
+// coil's plane (the tile's rows of Tz cells) at an odd stride in cells.
+__host__ __device__ inline size_t cmtile_smem(int ncell, int cbk) {
+    return sizeof(float2) * (size_t)(ncell | 1) * cbk;
+}
+
+// k2y from the coil-major grid through a shared tile of CBK coils at a time
+// (CBK a multiple of 4 dividing B): tile[bb * PS + row * Tz + z], PS the
+// plane stride (odd, so the lanes of a team, one per coil, read distinct
+// banks).  The tile is loaded a row at a time (a warp, or half a warp for
+// rows of at most 16 cells, reads one coil's row of Tz cells, coalesced).
+// Teams of G lanes (one point each, lanes over the chunk's coils) then
+// gather the Kronecker sums.  One block per gather sub-problem (a whole bin
+// unless it holds more than kGatherSub points).
+template <int DIM, int JM, int G>
+__global__ void __launch_bounds__(512) k2y_cmtile_kernel(Geom g, const float2* __restrict__ grid,
+                                                         float2* __restrict__ y, int CBK) {
+    static_assert(DIM == 2 || DIM == 3, "tiles of rows");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* tile = reinterpret_cast<float2*>(smem_raw);
+    const int4 sp = g.gsub[blockIdx.x];
+    int o[3];
+    tile_origin<DIM>(g, sp, o);
+    constexpr int DI = DIM - 1;
+    constexpr int DY = DIM - 2;
+    const int B = g.B;
+    const int Tz = g.T[DI], Ty = g.T[DY];
+    const int nrows = (DIM == 3) ? g.T[0] * g.T[1] : g.T[0];
+    const int PS = (nrows * Tz) | 1;
+    const int Kz = g.K[DI];
+    const size_t ibase = (size_t)sp.w * B;
+    const int nwarps = blockDim.x >> 5, warp = threadIdx.x >> 5, wl = threadIdx.x & 31;
+    const int ZW = (Tz <= 16) ? 16 : 32, RPW = 32 / ZW;
+    const int zl = wl % ZW, rsub = wl / ZW;
+    const bool zok = zl < Tz;
+    const int zoff = zok ? wrapn(o[DI] + zl, Kz) : 0;
+    const int team = threadIdx.x / G, lane = threadIdx.x % G, nteam = blockDim.x / G;
+    for (int b0 = 0; b0 < B; b0 += CBK) {
+        if (b0 > 0) __syncthreads();   // the previous chunk's gathers are done
+        for (int q = warp * RPW + rsub; q < CBK * nrows; q += nwarps * RPW) {
+            const int bb = q / nrows, r = q - bb * nrows;
+            size_t row;
+            if constexpr (DIM == 3) {
+                const int rx = r / g.T[1], ry = r - rx * g.T[1];
+                row = (size_t)wrapn(o[0] + rx, g.K[0]) * g.K[1] + wrapn(o[1] + ry, g.K[1]);
+            } else {
+                row = (size_t)wrapn(o[0] + r, g.K[0]);
+            }
+            if (zok)
+                tile[bb * PS + r * Tz + zl] =
+                    __ldg(grid + (ibase + b0 + bb) * (size_t)g.prodK + row * Kz + zoff);
+        }
+        __syncthreads();
+        for (int s = sp.y + team; s < sp.y + sp.z; s += nteam) {
+            float2 cz[JM], cy[JM];
+            {
+                const float2* src = g.coef[DI] + (size_t)s * g.JP[DI];
+#pragma unroll
+                for (int k = 0; k < JM; ++k) cz[k] = __ldg(src + k);
+                const float2* srcy = g.coef[DY] + (size_t)s * g.JP[DY];
+#pragma unroll
+                for (int j = 0; j < JM; ++j) cy[j] = __ldg(srcy + j);
+            }
+            const int lz = __ldg(g.pos[DI] + s) - o[DI];
+            const int ly = __ldg(g.pos[DY] + s) - o[DY];
+            const int lx = (DIM == 3) ? __ldg(g.pos[0] + s) - o[0] : 0;
+            const float2* c0src = g.coef[0] + (size_t)s * g.JP[0];
+            const int m = __ldg(g.perm + s);
+            for (int bb = lane; bb < CBK; bb += G) {
+                float2 acc = make_float2(0.f, 0.f);
+                const float2* tb = tile + bb * PS + lz;
+                if constexpr (DIM == 2) {
+#pragma unroll
+                    for (int j = 0; j < JM; ++j) {
+                        const float2* row = tb + (ly + j) * Tz;
+                        float2 t = make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int k = 0; k < JM; ++k) cfma(t, cz[k], row[k]);
+                        cfma(acc, cy[j], t);
+                    }
+                } else {
+#pragma unroll 1
+                    for (int i = 0; i < JM; ++i) {
+                        const float2* pl = tb + ((lx + i) * Ty + ly) * Tz;
+                        float2 ti = make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int j = 0; j < JM; ++j) {
+                            const float2* row = pl + j * Tz;
+                            float2 t = make_float2(0.f, 0.f);
+#pragma unroll
+                            for (int k = 0; k < JM; ++k) cfma(t, cz[k], row[k]);
+                            cfma(ti, cy[j], t);
+                        }
+                        cfma(acc, __ldg(c0src + i), ti);
+                    }
+                }
+                y[(size_t)m * B + b0 + bb] = acc;
+            }
+        }
+    }
+}
+
+}  // namespace nufft

@@ -81,7 +81,7 @@ static void k2y_launch(const Geom& g, const float2* grid, float2* y, cudaStream_
                     exact ? k2y_ctile_kernel<DIM, JM, G, true> : k2y_ctile_kernel<DIM, JM, G, false>;
                 if (smem > 48 * 1024)
                     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                kern<<<(unsigned)g.nsub, 512, smem, s>>>(g, grid, y);
+                kern<<<(unsigned)(g.gsub ? g.ngsub : g.nsub), 512, smem, s>>>(g, grid, y);
                 return;
             }
         }

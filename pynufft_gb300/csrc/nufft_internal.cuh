@@ -16,6 +16,23 @@
 
 namespace nufft {
 
+// Exact gridding: per-block partial sums of |re y| + |im y| reduced before the
+// fixed-point scale is fixed; the scale buffer holds [sum |y|, scale,
+// partials...].
+constexpr int kAbsSumParts = 1024;
+constexpr int kScaleSlots = 2 + kAbsSumParts;
+
+// Most points of one sub-problem of the gather list (interpolation from a
+// shared tile, plans of 8 or more coils): a bin's tile is loaded once unless
+// the bin holds more.
+constexpr int kGatherSub = 512;
+
+// Row gridding (plans of 8 or more coils): a sub-problem takes up to
+// kRowGroup consecutive bins along the innermost axis (3D) and at most
+// kRowSub points, so the tile's halo along that axis is shared.
+constexpr int kRowGroup = 4;
+constexpr int kRowSub = 512;
+
 void set_error(const std::string& msg);
 
 // Plan-time numerics of one axis (plan_math.cpp).
@@ -57,6 +74,12 @@ struct Geom {
     const float* wpt;            // per point prod_d max_j |coef|, sorted order
     const int4* sub;             // gridding sub-problems: (bin, start, count, inst)
     int64_t nsub;
+    int maxsub;                  // most points in one sub-problem
+    const int4* gsub;            // gather sub-problems (plans of 8+ coils): bins split
+    int64_t ngsub;               //   only past kGatherSub points
+    const int4* rsub;            // row-gridding sub-problems (plans of 8+ coils):
+    int64_t nrsub;               //   runs of <= kRowGroup bins along the innermost
+    int rgroup;                  //   axis (rgroup bins), <= kRowSub points
     int kmethod;                 // k2y lane mapping (NUFFT_K2Y_*), resolved
     int ymethod;                 // y2k lane mapping (NUFFT_Y2K_*), resolved
     int* kerr;                   // device flag: a bounded wait ran out (nufft_plan_check)
@@ -140,6 +163,11 @@ struct nufft_plan_s {
     float2* d_coef = nullptr;         // sum_d M * JP[d]
     int4* d_sub = nullptr;
     int64_t nsub = 0;
+    int4* d_gsub = nullptr;           // gather sub-problems (B >= 8)
+    int64_t ngsub = 0;
+    int4* d_rsub = nullptr;           // row-gridding sub-problems (B >= 8)
+    int64_t nrsub = 0;
+    int rgroup = 1;                   // bins per row sub-problem along the innermost axis
     int64_t nbins_total = 0;
     float wmax = 0.f;                 // max over points of prod_d max_j |coef|
 
@@ -225,6 +253,11 @@ void kernel_time_clear(nufft_plan_s* p);     // forget the records, keep the eve
 void kernel_time_destroy(nufft_plan_s* p);   // free the events
 int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s,
                bool pre_zeroed = false);   // pre_zeroed: grid already zero (fast mode)
+// coil-major spectra (plans of 8 or more coils, interp_cm.cuh): whether the
+// plan's geometry has the row kernels, and the two stages on p->d_cm layout
+bool cm_path(const nufft_plan_s* p);
+int launch_k2y_cm(nufft_plan_s* p, const float2* grid_cm, float2* y, cudaStream_t s);
+int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s);
 
 // fftstage.cu
 int launch_scale(const nufft_plan_s* p, const float2* in, float2* out, cudaStream_t s);
@@ -237,6 +270,9 @@ int forward_from_image(nufft_plan_s* p, const float2* xx, bool apply_sn, float2*
                        cudaStream_t s);
 int image_from_spectrum_coils(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn,
                               bool divide_sn, cudaStream_t s);
+// several coils, coil-major spectra in p->d_cm: image -> spectra / spectra -> image
+int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s);
+int cm_to_image(nufft_plan_s* p, float2* xx, bool apply_sn, bool divide_sn, cudaStream_t s);
 int launch_pad_sense(const nufft_plan_s* p, const float2* x, float2* grid, cudaStream_t s);
 int launch_crop_sense(const nufft_plan_s* p, const float2* grid, float2* x, cudaStream_t s);
 int fft_init(nufft_plan_s* p);

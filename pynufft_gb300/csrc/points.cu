@@ -410,6 +410,50 @@ __global__ void sub_fill_kernel(const int* __restrict__ bin_start, const int* __
     }
 }
 
+// Row-gridding sub-problems: along each line of bins of the innermost axis
+// (one thread per line), runs of up to `group` consecutive bins holding at
+// most `maxsub` points in all; a bin holding more is split into chunks of
+// maxsub on its own.  count pass (out == nullptr) or fill pass.
+__global__ void rowsub_kernel(const int* __restrict__ bin_start, int64_t nlines, int nbz,
+                              int group, int maxsub, int64_t nbin_inst,
+                              const int* __restrict__ line_start, int* __restrict__ line_count,
+                              int4* __restrict__ out) {
+    for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < nlines;
+         l += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b0 = l * nbz;
+        int n = 0;
+        int w = out ? line_start[l] : 0;
+        int bz = 0;
+        while (bz < nbz) {
+            const int64_t b = b0 + bz;
+            const int c = bin_start[b + 1] - bin_start[b];
+            if (c > maxsub) {   // a dense bin on its own, in chunks
+                for (int k = 0; k * maxsub < c; ++k) {
+                    if (out)
+                        out[w + n] = make_int4((int)b, bin_start[b] + k * maxsub,
+                                               min(maxsub, c - k * maxsub), (int)(b / nbin_inst));
+                    ++n;
+                }
+                ++bz;
+                continue;
+            }
+            int tot = c, e = bz + 1;
+            while (e < nbz && e - bz < group) {
+                const int ce = bin_start[b0 + e + 1] - bin_start[b0 + e];
+                if (ce > maxsub || tot + ce > maxsub) break;
+                tot += ce;
+                ++e;
+            }
+            if (tot > 0) {
+                if (out) out[w + n] = make_int4((int)b, bin_start[b], tot, (int)(b / nbin_inst));
+                ++n;
+            }
+            bz = e;
+        }
+        if (!out) line_count[l] = n;
+    }
+}
+
 void free_points(nufft_plan_s* p) {
     cudaFree(p->d_inst_start); p->d_inst_start = nullptr;
     cudaFree(p->d_perm); p->d_perm = nullptr;
@@ -417,6 +461,10 @@ void free_points(nufft_plan_s* p) {
     cudaFree(p->d_wpt); p->d_wpt = nullptr;
     cudaFree(p->d_coef); p->d_coef = nullptr;
     cudaFree(p->d_sub); p->d_sub = nullptr;
+    cudaFree(p->d_gsub); p->d_gsub = nullptr;
+    p->ngsub = 0;
+    cudaFree(p->d_rsub); p->d_rsub = nullptr;
+    p->nrsub = 0;
     cudaFree(p->d_ybuf); p->d_ybuf = nullptr;
     p->ybuf_elems = 0;
     p->M = 0;
@@ -493,6 +541,7 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     double* d_om = nullptr;
     int *d_bin_of = nullptr, *d_rank = nullptr, *d_cnt = nullptr, *d_start = nullptr;
     int *d_nsub = nullptr, *d_subst = nullptr, *d_err = nullptr, *d_bucket = nullptr;
+    int *d_gnsub = nullptr, *d_gsubst = nullptr, *d_rnl = nullptr, *d_rst = nullptr;
     int* d_slot = nullptr;
     unsigned int* d_wmax = nullptr;
     AxisTab* d_tab = nullptr;
@@ -503,6 +552,7 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
         cudaFree(d_ctab); d_ctab = nullptr;
         cudaFree(d_bin_of); cudaFree(d_rank); cudaFree(d_cnt); cudaFree(d_start);
         cudaFree(d_nsub); cudaFree(d_subst); cudaFree(d_err); cudaFree(d_wmax);
+        cudaFree(d_gnsub); cudaFree(d_gsubst); cudaFree(d_rnl); cudaFree(d_rst);
         cudaFree(d_bucket); cudaFree(d_slot);
     };
 #define TRY_TMP(expr)                                                              \
@@ -607,9 +657,36 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     TRY_TMP(cudaGetLastError());
     scan_kernel<<<1, 1024, 0, s>>>(d_nsub, d_subst, nbins);
     TRY_TMP(cudaGetLastError());
-    int h_nsub = 0, h_err = 0;
+    // gather list (interpolation from shared tiles of several coils): bins
+    // split only past kGatherSub points, so a tile is loaded once per bin
+    const bool glist = p->B >= 8;
+    // row-gridding list: lines of bins along the innermost axis
+    const int nbz = nb[nd - 1];
+    const int64_t nlines = nbins / nbz;
+    p->rgroup = (nd == 3) ? kRowGroup : 1;
+    const int lblocks = (int)std::min<int64_t>((nlines + threads - 1) / threads, 65535);
+    if (glist) {
+        TRY_TMP(cudaMalloc(&d_gnsub, sizeof(int) * nbins));
+        TRY_TMP(cudaMalloc(&d_gsubst, sizeof(int) * (nbins + 1)));
+        sub_count_kernel<<<bblocks, threads, 0, s>>>(d_start, nbins, kGatherSub, d_gnsub);
+        TRY_TMP(cudaGetLastError());
+        scan_kernel<<<1, 1024, 0, s>>>(d_gnsub, d_gsubst, nbins);
+        TRY_TMP(cudaGetLastError());
+        TRY_TMP(cudaMalloc(&d_rnl, sizeof(int) * nlines));
+        TRY_TMP(cudaMalloc(&d_rst, sizeof(int) * (nlines + 1)));
+        rowsub_kernel<<<lblocks, threads, 0, s>>>(d_start, nlines, nbz, p->rgroup, kRowSub,
+                                                  nbin_inst, nullptr, d_rnl, nullptr);
+        TRY_TMP(cudaGetLastError());
+        scan_kernel<<<1, 1024, 0, s>>>(d_rnl, d_rst, nlines);
+        TRY_TMP(cudaGetLastError());
+    }
+    int h_nsub = 0, h_gnsub = 0, h_rnsub = 0, h_err = 0;
     unsigned int h_wmax = 0;
     TRY_TMP(cudaMemcpyAsync(&h_nsub, d_subst + nbins, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (glist) {
+        TRY_TMP(cudaMemcpyAsync(&h_gnsub, d_gsubst + nbins, sizeof(int), cudaMemcpyDeviceToHost, s));
+        TRY_TMP(cudaMemcpyAsync(&h_rnsub, d_rst + nlines, sizeof(int), cudaMemcpyDeviceToHost, s));
+    }
     TRY_TMP(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     TRY_TMP(cudaMemcpyAsync(&h_wmax, d_wmax, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
     TRY_TMP(cudaStreamSynchronize(s));
@@ -628,6 +705,22 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
         sub_fill_kernel<<<bblocks, threads, 0, s>>>(d_start, d_subst, nbins, p->maxsub, nbin_inst,
                                                     p->d_sub);
         TRY_TMP(cudaGetLastError());
+    }
+    if (glist) {
+        p->ngsub = h_gnsub;
+        TRY_TMP(cudaMalloc(&p->d_gsub, sizeof(int4) * std::max(h_gnsub, 1)));
+        if (h_gnsub > 0) {
+            sub_fill_kernel<<<bblocks, threads, 0, s>>>(d_start, d_gsubst, nbins, kGatherSub,
+                                                        nbin_inst, p->d_gsub);
+            TRY_TMP(cudaGetLastError());
+        }
+        p->nrsub = h_rnsub;
+        TRY_TMP(cudaMalloc(&p->d_rsub, sizeof(int4) * std::max(h_rnsub, 1)));
+        if (h_rnsub > 0) {
+            rowsub_kernel<<<lblocks, threads, 0, s>>>(d_start, nlines, nbz, p->rgroup, kRowSub,
+                                                      nbin_inst, d_rst, nullptr, p->d_rsub);
+            TRY_TMP(cudaGetLastError());
+        }
     }
     TRY_TMP(cudaStreamSynchronize(s));
     cleanup();

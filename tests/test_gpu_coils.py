@@ -1,0 +1,78 @@
+"""Plans of 8 or more coils: forward / adjoint / selfadjoint keep the
+oversampled spectra coil-major and run the row-register gridding and the
+coil-major tile interpolation (interp_cm.cuh).  Against the oracle (one
+single-coil reference transform per coil, linalg/nufft_hsa.py:203-228 batch
+semantics) at 1e-5 relative L2, for 2D and 3D, J in {4, 6, 8}, 8 to 32
+coils, one or several instances, clustered points (bins split into several
+sub-problems), both gridding modes; the deterministic mode bitwise
+repeatable."""
+import numpy as np
+import pytest
+
+from oracle.nufft_oracle import OracleNUFFT, rel_l2
+from tests_util import cplx
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def _points(rng, M, ndim):
+    """Uniform points plus a dense cluster near the k-space centre (bins of
+    more than one sub-problem) and a few on the +-pi edges (wrapped tiles)."""
+    om = rng.uniform(-np.pi, np.pi, (M, ndim))
+    om[: M // 2] = rng.normal(0.0, 0.05, (M // 2, ndim))
+    om[-4:] = np.pi * np.array([[1.0], [-1.0], [0.999], [-0.999]])
+    return om
+
+
+CASES = [((24, 20), (48, 40), 6, 8), ((24, 20), (48, 40), 4, 32), ((20, 24), (40, 48), 8, 16),
+         ((24, 20), (48, 40), 6, 24), ((12, 14, 10), (24, 28, 20), 6, 8),
+         ((12, 14, 10), (24, 28, 20), 4, 32), ((10, 10, 10), (20, 20, 20), 8, 16)]
+
+
+@pytest.mark.parametrize('Nd,Kd,J,B', CASES)
+@pytest.mark.parametrize('det', [False, True])
+def test_coil_major_transforms_match_oracle(Nd, Kd, J, B, det):
+    from pynufft_gb300 import NUFFT
+    rng = np.random.default_rng(81)
+    M = 3000
+    Jd = (J,) * len(Nd)
+    om = _points(rng, M, len(Nd))
+    A = NUFFT(0)
+    A.plan(om, Nd, Kd, Jd, batch=B, deterministic=det)
+    O = OracleNUFFT()
+    O.plan(om, Nd, Kd, Jd, batch=B)
+    x = cplx(rng, Nd + (B,))
+    y = cplx(rng, (M, B))
+    ef = rel_l2(A.forward(x), O.forward(x))
+    xa = A.adjoint(y)
+    ea = rel_l2(xa, O.adjoint(y))
+    es = rel_l2(A.selfadjoint(x), O.selfadjoint(x))
+    assert max(ef, ea, es) < TOL, (ef, ea, es)
+    if det:
+        assert np.array_equal(xa, A.adjoint(y))
+    A.check()
+
+
+@pytest.mark.parametrize('ndim,B', [(2, 8), (3, 8), (2, 32)])
+def test_coil_major_many_instances_match_oracle(ndim, B):
+    from pynufft_gb300 import NUFFT
+    rng = np.random.default_rng(82)
+    Nd, Kd = ((24, 20), (48, 40)) if ndim == 2 else ((12, 12, 10), (24, 24, 20))
+    Jd = (6,) * ndim
+    Ms = [900, 1, 2500]
+    oms = [_points(rng, m, ndim) if m > 8 else rng.uniform(-np.pi, np.pi, (m, ndim)) for m in Ms]
+    A = NUFFT(0)
+    A.plan_many(oms, Nd, Kd, Jd, batch=B)
+    x = cplx(rng, (len(Ms),) + Nd + (B,))
+    y = cplx(rng, (sum(Ms), B))
+    yf = A.forward(x)
+    xa = A.adjoint(y)
+    off = 0
+    for i, om in enumerate(oms):
+        O = OracleNUFFT()
+        O.plan(om, Nd, Kd, Jd, batch=B)
+        sl = slice(off, off + Ms[i])
+        assert rel_l2(yf[sl], O.forward(x[i])) < TOL, i
+        assert rel_l2(xa[i], O.adjoint(y[sl])) < TOL, i
+        off += Ms[i]

@@ -55,13 +55,15 @@ def test_stages_match_reference(NUFFT, case):
 @pytest.mark.parametrize('case', ['plan_2d', 'plan_3d', 'plan_1d'])
 def test_solve_cg_matches_reference(NUFFT, case):
     """solve(y, 'cg', maxiter=5): float32 vectors with FP64 scalars against
-    scipy's complex128 CG; 5 iterations keep the round-off growth small."""
+    scipy's complex128 CG.  At 5 iterations the recursion barely amplifies
+    the operator's float32 rounding (the oracle with a complex64-rounded
+    operator lands ~5e-8 from the reference here), so the parity bar holds."""
     g = load_golden(case)
     A = NUFFT(0)
     A.plan(g['om'], _tup(g['Nd']), _tup(g['Kd']), _tup(g['Jd']))
     x, it = A.solve(g['y'], 'cg', maxiter=5, return_info=True)
     assert it == 5
-    assert rel_l2(x, g['solve_cg5']) < 1e-4, rel_l2(x, g['solve_cg5'])
+    assert rel_l2(x, g['solve_cg5']) < TOL, rel_l2(x, g['solve_cg5'])
 
 
 def test_radial_c1_matches_reference(NUFFT):
@@ -379,7 +381,7 @@ def test_cg_on_many_instances_and_coils_matches_oracle(NUFFT):
             if i == 1 and b == 1:
                 assert not np.any(x[i][..., b])
             else:
-                assert rel_l2(x[i][..., b], xo[..., b]) < 1e-4
+                assert rel_l2(x[i][..., b], xo[..., b]) < TOL
         off += Ms[i]
 
 
