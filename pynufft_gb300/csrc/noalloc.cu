@@ -12,13 +12,19 @@
 // The scratch is a file-scope __device__ array of NUFFT_STATIC_SCRATCH_CELLS
 // grid cells (2 x 8 bytes each, i.e. 16 MiB) plus the scale reduction
 // buffers; every GPU that loads the library holds it until the process
-// exits.  Its device address is looked up once per device with
-// cudaGetSymbolAddress on the first call made while that device is current,
-// so make that first call before any stream capture.  All calls share the
-// array and it keeps the last call's contents (it is cleared at the start
-// of each call); calls whose work overlaps on the GPU -- on different
-// streams, or from different host threads -- race on it.
+// exits.  Host code cannot use the array's name as a device address, so the
+// address is looked up with cudaGetSymbolAddress on the first call made in
+// each CUDA context (with that context's device current) and kept for that
+// context; a new context on the device (after cudaDeviceReset, say) is seen
+// by its id and looked up again.  Make the first call on a device before any
+// stream capture.  All calls share the array and it keeps the last call's
+// contents (it is cleared at the start of each call); calls whose work
+// overlaps on the GPU -- on different streams, or from different host
+// threads -- race on it.
 #include "nufft_internal.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include <mutex>
 
@@ -30,40 +36,84 @@ int launch_y2k_exact_into(const nufft_plan_s* p, const float2* y, float2* grid,
 namespace {
 
 constexpr size_t kCells = NUFFT_STATIC_SCRATCH_CELLS;
-constexpr int kScal = 2 + 1024;   // scale, sum|y| and per-block partials
+constexpr int kScal = nufft::kScaleSlots;   // sum|y|, scale and the per-block partials
+static_assert(kScal >= 2 + nufft::kAbsSumParts, "scale buffer smaller than its partial sums");
 
 static __device__ __align__(256) unsigned long long g_acc[2 * kCells];
 static __device__ __align__(256) double g_scal[kScal];
 
 constexpr int kMaxDevices = 64;
+struct Scratch {
+    unsigned long long ctx_id = 0;   // context the addresses belong to (0: none yet)
+    unsigned long long* acc = nullptr;
+    double* scal = nullptr;
+};
 std::mutex g_mu;
-unsigned long long* g_acc_ptr[kMaxDevices] = {};
-double* g_scal_ptr[kMaxDevices] = {};
+Scratch g_scratch[kMaxDevices];
 
-// Device addresses of the scratch arrays for the current device.
-int scratch_for_current_device(unsigned long long** acc, double** scal) {
+// Id of the calling thread's current context (unique for the process's
+// lifetime, so a re-created context gets a new one), through driver entry
+// points fetched by the runtime (the library does not link libcuda).
+// Returns 0 if it cannot be found.
+unsigned long long current_context_id() {
+    static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+    static PFN_cuCtxGetId_v12000 get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void* f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(f);
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+    if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device addresses of the scratch arrays in the current device's context
+// (which must be the plan's device).
+int scratch_for_current_device(int plan_device, unsigned long long** acc, double** scal) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         nufft::set_error("nufft_y2k_exact_static: no usable current CUDA device");
         return NUFFT_ECUDA;
     }
+    if (dev != plan_device) {
+        nufft::set_error("nufft_y2k_exact_static: the plan's device (" +
+                         std::to_string(plan_device) + ") is not the current device (" +
+                         std::to_string(dev) + ")");
+        return NUFFT_EINVAL;
+    }
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_acc_ptr[dev]) {
+    Scratch& c = g_scratch[dev];
+    const unsigned long long ctx = current_context_id();
+    if (ctx == 0 || c.ctx_id != ctx) {
         void* a = nullptr;
-        void* c = nullptr;
+        void* b = nullptr;
         e = cudaGetSymbolAddress(&a, g_acc);
-        if (e == cudaSuccess) e = cudaGetSymbolAddress(&c, g_scal);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&b, g_scal);
         if (e != cudaSuccess) {
             nufft::set_error(std::string("nufft_y2k_exact_static: cudaGetSymbolAddress: ") +
                              cudaGetErrorString(e));
             return NUFFT_ECUDA;
         }
-        g_acc_ptr[dev] = static_cast<unsigned long long*>(a);
-        g_scal_ptr[dev] = static_cast<double*>(c);
+        c.acc = static_cast<unsigned long long*>(a);
+        c.scal = static_cast<double*>(b);
+        // the lookup made the runtime's context current if none was; an
+        // unknown id (0) means the next call looks the addresses up again
+        c.ctx_id = current_context_id();
     }
-    *acc = g_acc_ptr[dev];
-    *scal = g_scal_ptr[dev];
+    *acc = c.acc;
+    *scal = c.scal;
     return NUFFT_OK;
 }
 
@@ -91,7 +141,7 @@ extern "C" int nufft_y2k_exact_static(nufft_plan_t p, const void* y, void* k, vo
     }
     unsigned long long* acc = nullptr;
     double* scal = nullptr;
-    int st = scratch_for_current_device(&acc, &scal);
+    int st = scratch_for_current_device(p->device, &acc, &scal);
     if (st != NUFFT_OK) return st;
     return nufft::launch_y2k_exact_into(p, static_cast<const float2*>(y), static_cast<float2*>(k),
                                         acc, scal, reinterpret_cast<cudaStream_t>(stream));

@@ -4,20 +4,24 @@ hand all GPU memory to their own pool up front, or latency-critical code that
 cannot let cudaMalloc/cudaFree synchronise the device).
 
 It is called through the C ABI and compared with the existing entry point,
-nufft_y2k on a plan created in deterministic mode, on two calls in a row with
-different inputs, so the shared scratch must be cleared between calls.  This
-file is collected last so that a run stopping at the first failure has
-already run every other test."""
+nufft_y2k on a deterministic plan of the same points: both sum the same
+64-bit fixed-point contributions exactly with the same scale and round once,
+so the results must agree bit for bit.  Each case runs two calls in a row
+with different inputs, so scratch left over from the first call would show.
+The plan given to the static entry point may be of either mode, with one or
+several coils or instances; on two reference fixtures the result is also held
+to the oracle.  This file is collected last so that a run stopping at the
+first failure has already run every other test.
+"""
 import ctypes
 
 import numpy as np
 import pytest
 
 from conftest import load_golden
-from oracle.nufft_oracle import rel_l2
+from oracle.nufft_oracle import OracleNUFFT, rel_l2
 
 pytestmark = pytest.mark.gpu
-TOL = 1e-5
 
 
 def _ptr(t):
@@ -28,28 +32,52 @@ def _cplx(rng, shape):
     return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
 
 
-@pytest.mark.parametrize('case,batch', [('plan_2d', None), ('plan_3d', None), ('plan_2d', 3)])
-def test_no_alloc_gridding_matches_existing_entry_point(case, batch):
+def _geometry(case):
+    if case == 'instances':
+        rng = np.random.default_rng(71)
+        oms = [rng.uniform(-np.pi, np.pi, (m, 2)) for m in (900, 1, 2500, 300)]
+        return oms, (20, 24), (40, 48), (6, 6)
+    g = load_golden(case)
+    return [g['om']], tuple(int(v) for v in g['Nd']), tuple(int(v) for v in g['Kd']), \
+        tuple(int(v) for v in g['Jd'])
+
+
+def _plan(NUFFT, oms, Nd, Kd, Jd, batch, det):
+    A = NUFFT(0)
+    if len(oms) > 1:
+        A.plan_many(oms, Nd, Kd, Jd, batch=batch, deterministic=det)
+    else:
+        A.plan(oms[0], Nd, Kd, Jd, batch=batch, deterministic=det)
+    return A
+
+
+@pytest.mark.parametrize('case,batch,det', [('plan_2d', None, True), ('plan_3d', None, True),
+                                            ('plan_2d', 3, True), ('plan_2d', None, False),
+                                            ('plan_3d', 8, False), ('plan_2d', 32, False),
+                                            ('instances', None, False), ('instances', 2, True)])
+def test_no_alloc_gridding_matches_existing_entry_point(case, batch, det):
     import torch
     from pynufft_gb300 import NUFFT, _lib
     lib = _lib.load()
-    g = load_golden(case)
-    Nd, Kd, Jd = (tuple(int(v) for v in g[k]) for k in ('Nd', 'Kd', 'Jd'))
-    A = NUFFT(0)
-    A.plan(g['om'], Nd, Kd, Jd, batch=batch, deterministic=True)
+    oms, Nd, Kd, Jd = _geometry(case)
+    A = _plan(NUFFT, oms, Nd, Kd, Jd, batch, det)       # given to the static entry point
+    R = _plan(NUFFT, oms, Nd, Kd, Jd, batch, True)      # deterministic nufft_y2k
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     rng = np.random.default_rng(5)
     for call in range(2):
         y = torch.from_numpy(_cplx(rng, A._shape('y'))).cuda()
         want = torch.empty(A._shape('k'), dtype=torch.complex64, device='cuda')
         got = torch.full(A._shape('k'), float('nan'), dtype=torch.complex64, device='cuda')
-        assert lib.nufft_y2k(A._plan, _ptr(y), _ptr(want), stream) == _lib.NUFFT_OK
+        assert lib.nufft_y2k(R._plan, _ptr(y), _ptr(want), stream) == _lib.NUFFT_OK
         st = lib.nufft_y2k_exact_static(A._plan, _ptr(y), _ptr(got), stream)
         assert st == _lib.NUFFT_OK, lib.nufft_last_error()
         torch.cuda.synchronize()
-        w, gt = want.cpu().numpy(), got.cpu().numpy()
-        assert np.all(np.isfinite(gt)), call
-        assert rel_l2(gt, w) < TOL, (call, rel_l2(gt, w))
+        assert torch.equal(got, want), (call, rel_l2(got.cpu().numpy(), want.cpu().numpy()))
+        if case.startswith('plan_') and batch is None:
+            O = OracleNUFFT()
+            O.plan(oms[0], Nd, Kd, Jd)
+            e = rel_l2(got.cpu().numpy(), O.y2k(y.cpu().numpy()))
+            assert e < 1e-6, (call, e)
 
 
 def test_no_alloc_gridding_rejects_a_grid_beyond_its_scratch():
