@@ -374,7 +374,8 @@ def batched_leg(torch, dev, peak, steps):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=200)
+    ap.add_argument('--steps', type=int, default=None,
+                    help='timed steps (default 200 on the GPU, 5 full pairs for the CPU reference)')
     ap.add_argument('--warmup', type=int, default=5)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--config', default='c2', choices=sorted(CONFIGS))
@@ -385,6 +386,8 @@ def main():
     ap.add_argument('--batched-only', action='store_true',
                     help='print only the multi-coil leg (a development aid; not a bench line)')
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 5 if args.impl == 'reference' else 200
     args.warmup = max(args.warmup, 3)
 
     world = int(os.environ.get('WORLD_SIZE', '1'))

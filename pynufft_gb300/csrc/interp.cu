@@ -18,8 +18,6 @@ int y2k_dim2(int jm, bool det, const Geom& g, const float2* y, float2* grid,
              unsigned long long* igrid, const double* dscal, cudaStream_t s);
 int y2k_dim3(int jm, bool det, const Geom& g, const float2* y, float2* grid,
              unsigned long long* igrid, const double* dscal, cudaStream_t s);
-int k2y_cm_dim2(int jm, const Geom& g, const float2* grid, float2* y, cudaStream_t s);
-int k2y_cm_dim3(int jm, const Geom& g, const float2* grid, float2* y, cudaStream_t s);
 int y2k_cm_dim2(int jm, bool det, const Geom& g, const float2* y, float2* grid,
                 unsigned long long* igrid, const double* dscal, cudaStream_t s);
 int y2k_cm_dim3(int jm, bool det, const Geom& g, const float2* y, float2* grid,
@@ -194,12 +192,17 @@ int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s, b
 // coil-major spectra (plans of 8 or more coils)
 // ---------------------------------------------------------------------------
 // The row kernels are built for J in {4, 6, 8} on every axis, B a multiple
-// of 8, and the default bins of such plans (innermost extent 16 in 2D, 8 in
-// 3D); tiles must not wrap onto themselves and the gather's tile of at least
-// four coils must fit in shared memory.
+// of 8 (of 32 in 2D), and the default bins of such plans (rows of 16 cells:
+// one 16-cell bin in 2D, four 4-cell bins in 3D); tiles must not wrap onto
+// themselves.
 bool cm_path(const nufft_plan_s* p) {
     if (p->B < 8 || p->B % 8 != 0 || (p->ndim != 2 && p->ndim != 3) || !p->d_cm || !p->d_rsub)
         return false;
+    // 2D rows hold one coil per lane only with a multiple of 32 coils; with
+    // four rows of 8 coils per warp the 2D tiles' few points per row block
+    // leave the coil-team kernel faster (2D spiral, 8 coils: 0.05 against
+    // 0.12 ms)
+    if (p->ndim == 2 && p->B % 32 != 0) return false;
     const int J = p->Jd[0];
     if (J != 4 && J != 6 && J != 8) return false;
     const int DI = p->ndim - 1;
@@ -211,16 +214,6 @@ bool cm_path(const nufft_plan_s* p) {
     if (p->bs[DI] * p->rgroup != 16 || 16 + J - 1 > p->Kd[DI]) return false;
     const int nkey = p->bs[0] * (p->ndim == 3 ? p->bs[1] : 1);
     return nkey <= 256 && rows_smem(p->ndim, J, nkey, kRowSub, 8) <= 200 * 1024;
-}
-
-int launch_k2y_cm(nufft_plan_s* p, const float2* grid_cm, float2* y, cudaStream_t s) {
-    if (p->M == 0) return NUFFT_OK;
-    Geom g = p->geom();
-    const int jm = pick_jm(p);
-    const bool timed = kernel_time_start(p, 0, s);
-    const int st = (p->ndim == 2) ? k2y_cm_dim2(jm, g, grid_cm, y, s) : k2y_cm_dim3(jm, g, grid_cm, y, s);
-    kernel_time_stop(p, 0, s, timed);
-    return st;
 }
 
 int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s) {

@@ -1,32 +1,26 @@
-// Coil-major interpolation and gridding for plans of 8 or more coils.
+// Coil-major gridding for plans of 8 or more coils.
 //
-// The forward and adjoint transforms of a multi-coil plan keep the
-// oversampled spectra coil-major -- grid_cm[(inst * B + b) * prod(Kd) + cell]
-// -- from the FFTs through the interpolation / gridding, so the spectra need
-// no coil-fastest copy.  (The reference's batch layout, coil fastest in
-// x / k / y, linalg/nufft_hsa.py:203-228, is kept at the API: images and
-// samples stay coil-fastest; only the internal spectra are coil-major.)
+// The adjoint of a multi-coil plan grids straight into coil-major spectra --
+// grid_cm[(inst * B + b) * prod(Kd) + cell] -- the layout its inverse FFTs
+// read, so the gridded spectra need no transpose.  (The reference's batch
+// layout, coil fastest in x / k / y, linalg/nufft_hsa.py:203-228, is kept at
+// the API: images and samples stay coil-fastest.)
 //
-// Gridding (y2k_rows_kernel).  A block takes one sub-problem (a chunk of one
-// bin's points) and the tile (bin + J-1 halo) it scatters to.  The tile is
-// cut into "rows" along the innermost axis (Tz cells each); a warp holds the
-// sums of RS rows x CB coils in registers (lane = row slot x coil, TZ
-// complex accumulators per lane) and visits, in a fixed order, every point
-// whose footprint crosses those rows: u = y conj(c_x c_y) for its row, then
-// the J innermost taps acc[pz + k] += u conj(c_z[k]) at register indices
-// chosen by a warp-uniform switch on pz.  No shared-memory atomics and no
-// float-to-integer conversions per tap; the rows' sums are flushed once per
-// row block through a per-warp shared transpose, so each (row, coil) goes
-// out as a contiguous run of Tz cells: float2 atomics into the grid (fast
-// mode), or 64-bit fixed-point integer atomics (deterministic mode: the
-// per-row float sums are a fixed-order reduction, their combination across
-// tiles is exact, so the result is bitwise reproducible).
-//
-// Interpolation (k2y_cmtile_kernel).  The block loads its sub-problem's tile
-// for a chunk of CBK coils from the coil-major grid into shared memory with
-// the coils fastest (each thread reads runs of four cells of one coil's row
-// and writes them coil-fastest), then teams of G lanes (one point each,
-// lanes over coils) gather the Kronecker sums from the tile.
+// Gridding (y2k_rows_kernel).  A block takes one row sub-problem (the points
+// of one bin, or of up to four consecutive bins along the innermost axis in
+// 3D) and the tile (bins + J-1 halo) it scatters to.  The tile is cut into
+// "rows" along the innermost axis (TZ cells each); a warp holds the sums of
+// RS rows x CB coils in registers (lane = row slot x coil, TZ complex
+// accumulators per lane) and visits, in a fixed order, every point whose
+// footprint crosses those rows: u = y conj(c_x c_y) for its row, then the J
+// innermost taps acc[pz + k] += u conj(c_z[k]) at register indices chosen by
+// a warp-uniform switch on pz.  The points' coefficients and offsets are
+// staged in shared memory first, sorted by row.  No shared-memory atomics
+// and no float-to-integer conversions per tap; each lane's row is flushed
+// once per row block: float2 atomics into the grid (fast mode), or 64-bit
+// fixed-point integer atomics (deterministic mode: the per-row float sums
+// are a fixed-order reduction, their combination across tiles is exact, so
+// the result is bitwise reproducible).
 #pragma once
 #include "interp.cuh"
 
@@ -266,108 +260,6 @@ __global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __r
                 } else {
                     atomicAdd(grid + e, v);
                 }
-            }
-        }
-    }
-}
-
-// Shared memory of k2y_cmtile_kernel (bytes): the tile of CBK coils, each
-// coil's plane (the tile's rows of Tz cells) at an odd stride in cells.
-__host__ __device__ inline size_t cmtile_smem(int ncell, int cbk) {
-    return sizeof(float2) * (size_t)(ncell | 1) * cbk;
-}
-
-// k2y from the coil-major grid through a shared tile of CBK coils at a time
-// (CBK a multiple of 4 dividing B): tile[bb * PS + row * Tz + z], PS the
-// plane stride (odd, so the lanes of a team, one per coil, read distinct
-// banks).  The tile is loaded a row at a time (a warp, or half a warp for
-// rows of at most 16 cells, reads one coil's row of Tz cells, coalesced).
-// Teams of G lanes (one point each, lanes over the chunk's coils) then
-// gather the Kronecker sums.  One block per gather sub-problem (a whole bin
-// unless it holds more than kGatherSub points).
-template <int DIM, int JM, int G>
-__global__ void __launch_bounds__(512) k2y_cmtile_kernel(Geom g, const float2* __restrict__ grid,
-                                                         float2* __restrict__ y, int CBK) {
-    static_assert(DIM == 2 || DIM == 3, "tiles of rows");
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2* tile = reinterpret_cast<float2*>(smem_raw);
-    const int4 sp = g.gsub[blockIdx.x];
-    int o[3];
-    tile_origin<DIM>(g, sp, o);
-    constexpr int DI = DIM - 1;
-    constexpr int DY = DIM - 2;
-    const int B = g.B;
-    const int Tz = g.T[DI], Ty = g.T[DY];
-    const int nrows = (DIM == 3) ? g.T[0] * g.T[1] : g.T[0];
-    const int PS = (nrows * Tz) | 1;
-    const int Kz = g.K[DI];
-    const size_t ibase = (size_t)sp.w * B;
-    const int nwarps = blockDim.x >> 5, warp = threadIdx.x >> 5, wl = threadIdx.x & 31;
-    const int ZW = (Tz <= 16) ? 16 : 32, RPW = 32 / ZW;
-    const int zl = wl % ZW, rsub = wl / ZW;
-    const bool zok = zl < Tz;
-    const int zoff = zok ? wrapn(o[DI] + zl, Kz) : 0;
-    const int team = threadIdx.x / G, lane = threadIdx.x % G, nteam = blockDim.x / G;
-    for (int b0 = 0; b0 < B; b0 += CBK) {
-        if (b0 > 0) __syncthreads();   // the previous chunk's gathers are done
-        for (int q = warp * RPW + rsub; q < CBK * nrows; q += nwarps * RPW) {
-            const int bb = q / nrows, r = q - bb * nrows;
-            size_t row;
-            if constexpr (DIM == 3) {
-                const int rx = r / g.T[1], ry = r - rx * g.T[1];
-                row = (size_t)wrapn(o[0] + rx, g.K[0]) * g.K[1] + wrapn(o[1] + ry, g.K[1]);
-            } else {
-                row = (size_t)wrapn(o[0] + r, g.K[0]);
-            }
-            if (zok)
-                tile[bb * PS + r * Tz + zl] =
-                    __ldg(grid + (ibase + b0 + bb) * (size_t)g.prodK + row * Kz + zoff);
-        }
-        __syncthreads();
-        for (int s = sp.y + team; s < sp.y + sp.z; s += nteam) {
-            float2 cz[JM], cy[JM];
-            {
-                const float2* src = g.coef[DI] + (size_t)s * g.JP[DI];
-#pragma unroll
-                for (int k = 0; k < JM; ++k) cz[k] = __ldg(src + k);
-                const float2* srcy = g.coef[DY] + (size_t)s * g.JP[DY];
-#pragma unroll
-                for (int j = 0; j < JM; ++j) cy[j] = __ldg(srcy + j);
-            }
-            const int lz = __ldg(g.pos[DI] + s) - o[DI];
-            const int ly = __ldg(g.pos[DY] + s) - o[DY];
-            const int lx = (DIM == 3) ? __ldg(g.pos[0] + s) - o[0] : 0;
-            const float2* c0src = g.coef[0] + (size_t)s * g.JP[0];
-            const int m = __ldg(g.perm + s);
-            for (int bb = lane; bb < CBK; bb += G) {
-                float2 acc = make_float2(0.f, 0.f);
-                const float2* tb = tile + bb * PS + lz;
-                if constexpr (DIM == 2) {
-#pragma unroll
-                    for (int j = 0; j < JM; ++j) {
-                        const float2* row = tb + (ly + j) * Tz;
-                        float2 t = make_float2(0.f, 0.f);
-#pragma unroll
-                        for (int k = 0; k < JM; ++k) cfma(t, cz[k], row[k]);
-                        cfma(acc, cy[j], t);
-                    }
-                } else {
-#pragma unroll 1
-                    for (int i = 0; i < JM; ++i) {
-                        const float2* pl = tb + ((lx + i) * Ty + ly) * Tz;
-                        float2 ti = make_float2(0.f, 0.f);
-#pragma unroll
-                        for (int j = 0; j < JM; ++j) {
-                            const float2* row = pl + j * Tz;
-                            float2 t = make_float2(0.f, 0.f);
-#pragma unroll
-                            for (int k = 0; k < JM; ++k) cfma(t, cz[k], row[k]);
-                            cfma(ti, cy[j], t);
-                        }
-                        cfma(acc, __ldg(c0src + i), ti);
-                    }
-                }
-                y[(size_t)m * B + b0 + bb] = acc;
             }
         }
     }

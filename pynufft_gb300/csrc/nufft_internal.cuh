@@ -253,10 +253,9 @@ void kernel_time_clear(nufft_plan_s* p);     // forget the records, keep the eve
 void kernel_time_destroy(nufft_plan_s* p);   // free the events
 int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s,
                bool pre_zeroed = false);   // pre_zeroed: grid already zero (fast mode)
-// coil-major spectra (plans of 8 or more coils, interp_cm.cuh): whether the
-// plan's geometry has the row kernels, and the two stages on p->d_cm layout
+// coil-major gridding (plans of 8 or more coils, interp_cm.cuh): whether the
+// plan's geometry has the row kernels, and y2k into the p->d_cm layout
 bool cm_path(const nufft_plan_s* p);
-int launch_k2y_cm(nufft_plan_s* p, const float2* grid_cm, float2* y, cudaStream_t s);
 int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s);
 
 // fftstage.cu

@@ -349,7 +349,7 @@ __global__ void build_tables_kernel(const double* __restrict__ om, int64_t M, in
                                     const int* __restrict__ rank_of,
                                     const int* __restrict__ bin_start,
                                     const int* __restrict__ bucket_count,
-                                    const int* __restrict__ slot,
+                                    const int* __restrict__ slot, int nkeys,
                                     int* __restrict__ perm, int* __restrict__ pos,
                                     float2* __restrict__ coef0, float2* __restrict__ coef1,
                                     float2* __restrict__ coef2, float* __restrict__ wpt,
@@ -359,11 +359,19 @@ __global__ void build_tables_kernel(const double* __restrict__ om, int64_t M, in
         const int bk = bin_of[m];
         if (bk < 0) continue;
         const int bin = bk >> 5, key = bk & 31, rank = rank_of[m];
-        // slot dealt by deal_bins_kernel, found from (key, rank)
+        // slot dealt by deal_bins_kernel, found from (key, rank); without a
+        // deal (slot == nullptr) the keys of the bin are interleaved round
+        // robin: (key, rank) follows every point of lower rank and the
+        // points of equal rank and lower key
         const int* c = bucket_count + (int64_t)bin * 32;
         int pre = 0;
-        for (int k = 0; k < key; ++k) pre += c[k];
-        const int64_t s = (int64_t)bin_start[bin] + slot[(int64_t)bin_start[bin] + pre + rank];
+        if (slot) {
+            for (int k = 0; k < key; ++k) pre += c[k];
+            pre = slot[(int64_t)bin_start[bin] + pre + rank];
+        } else {
+            for (int k = 0; k < nkeys; ++k) pre += min(rank, c[k]) + ((k < key && c[k] > rank) ? 1 : 0);
+        }
+        const int64_t s = (int64_t)bin_start[bin] + pre;
         perm[s] = (int)m;
         float wprod = 1.f;
         for (int d = 0; d < ndim; ++d) {
@@ -632,7 +640,12 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     float2* c1 = c0 + (nd > 1 ? Malloc * JP[0] : 0);
     float2* c2 = c1 + (nd > 2 ? Malloc * JP[1] : 0);
     const int bblocks = (int)std::min<int64_t>((nbins + threads - 1) / threads, 65535);
-    if (M > 0) {
+    // plans of 8 or more coils sort each sub-problem's points by row in the
+    // gridding kernel, and their gather teams take 32 / G points per warp:
+    // a round-robin interleave of the bank keys (in build_tables) replaces
+    // the deal, whose per-bin loop is long for the dense bins of such plans
+    const bool deal = p->B < 8;
+    if (M > 0 && deal) {
         deal_bins_kernel<<<bblocks, threads, 0, s>>>(d_bucket, d_start, nbins,
                                                      keys_in_use(nd, p->B), p->maxsub, d_slot);
         TRY_TMP(cudaGetLastError());
@@ -649,7 +662,9 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
         auto kern = (jm == 4) ? build_tables_kernel<4> : (jm == 6) ? build_tables_kernel<6>
                     : (jm == 8) ? build_tables_kernel<8> : build_tables_kernel<16>;
         kern<<<blocks, threads, 0, s>>>(d_om, M, nd, p->d_axc, d_tab, d_ctab, g, d_bin_of, d_rank,
-                                        d_start, d_bucket, d_slot, p->d_perm, p->d_pos, c0, c1, c2, p->d_wpt,
+                                        d_start, d_bucket, deal ? d_slot : nullptr,
+                                        keys_in_use(nd, p->B), p->d_perm,
+                                        p->d_pos, c0, c1, c2, p->d_wpt,
                                         d_wmax);
         TRY_TMP(cudaGetLastError());
     }

@@ -1,8 +1,9 @@
-"""Plans of 8 or more coils: forward / adjoint / selfadjoint keep the
-oversampled spectra coil-major and run the row-register gridding and the
-coil-major tile interpolation (interp_cm.cuh).  Against the oracle (one
-single-coil reference transform per coil, linalg/nufft_hsa.py:203-228 batch
-semantics) at 1e-5 relative L2, for 2D and 3D, J in {4, 6, 8}, 8 to 32
+"""Plans of 8 or more coils: forward / adjoint / selfadjoint through the
+coil-team kernels, the adjoint of 3D plans and of 2D plans with a multiple
+of 32 coils gridding by register rows straight into coil-major spectra
+(interp_cm.cuh), the others through the coil-team tile.  Against the oracle
+(one single-coil reference transform per coil, linalg/nufft_hsa.py:203-228
+batch semantics) at 1e-5 relative L2, for 2D and 3D, J in {4, 6, 8}, 8 to 32
 coils, one or several instances, clustered points (bins split into several
 sub-problems), both gridding modes; the deterministic mode bitwise
 repeatable."""
