@@ -1,7 +1,7 @@
 """Benchmark: NUFFT forward+adjoint pairs/s on one GB300 (per GPU, replicas).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--config c1|c2|c3|c4|c5]
+                    [--config c1|c2|c3|c3i|c4|c5|c5s]
 
 Default workload (c2): 3D Nd 128^3, Kd 256^3, Jd 6^3, M = 2,000,000 points
 i.i.d. uniform in [-pi, pi)^3, complex64 image of 32 random ellipsoids.  One
@@ -63,6 +63,11 @@ CONFIGS = {
     'c3i': dict(name='64 independent 2D uniform instances, M ~ U{20000..200000} each, Nd 320^2, Kd 640^2, '
                      'Jd 6^2, one fwd+adj of every instance per step (a pair = one instance)',
                 Nd=(320, 320), Kd=(640, 640), Jd=(6, 6), batch=None, ninst=64),
+    # a small case of the kooshball workload (same points per cell), for
+    # kernel captures that must stay small
+    'c5s': dict(name='3D kooshball 3906x256 (M=999,936), Nd 96^3, Kd 192^3, Jd 6^3, 8 coils, fwd+adj pair '
+                     '(small case of the 8M-point kooshball)',
+                Nd=(96, 96, 96), Kd=(192, 192, 192), Jd=(6, 6, 6), batch=8),
 }
 
 
@@ -84,6 +89,9 @@ def workload(cfg: str):
     elif cfg == 'c3i':
         om = T.uneven_instances(c['ninst'], seed=5)
         x = T.random_image((c['ninst'],) + c['Nd'], seed=0)
+    elif cfg == 'c5s':
+        om = T.kooshball_3d(3906, 256)
+        x = T.random_image(c['Nd'] + (8,), seed=0)
     else:
         om = T.kooshball_3d(15625, 512)
         x = T.random_image(c['Nd'] + (8,), seed=0)
@@ -122,7 +130,7 @@ def bench_config(cfg, world=1):
 
 
 CONFIG_POINTS = {'c1': 256 * 512, 'c2': 2_000_000, 'c3': 400 * 640, 'c4': 32 * 2048,
-                 'c5': 15625 * 512, 'c3i': None}
+                 'c5': 15625 * 512, 'c3i': None, 'c5s': 3906 * 256}
 
 
 def alg_bytes(c, M):
@@ -385,6 +393,8 @@ def main():
                     help='timed pairs per measurement of the multi-coil leg')
     ap.add_argument('--batched-only', action='store_true',
                     help='print only the multi-coil leg (a development aid; not a bench line)')
+    ap.add_argument('--deterministic', action='store_true',
+                    help='plan the workload in the deterministic gridding mode')
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 5 if args.impl == 'reference' else 200
@@ -416,9 +426,11 @@ def main():
 
     def make_plan():
         if ninst > 1:
-            A.plan_many(om, c['Nd'], c['Kd'], c['Jd'], batch=c['batch'])
+            A.plan_many(om, c['Nd'], c['Kd'], c['Jd'], batch=c['batch'],
+                        deterministic=args.deterministic)
         else:
-            A.plan(om, c['Nd'], c['Kd'], c['Jd'], batch=c['batch'])
+            A.plan(om, c['Nd'], c['Kd'], c['Jd'], batch=c['batch'],
+                   deterministic=args.deterministic)
     make_plan()
     torch.cuda.synchronize()
     t0 = time.perf_counter()       # second plan: host om, tables rebuilt, no first-use costs
