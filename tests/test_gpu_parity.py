@@ -385,11 +385,12 @@ def test_cg_on_many_instances_and_coils_matches_oracle(NUFFT):
         off += Ms[i]
 
 
-@pytest.mark.parametrize('B', [None, 4])
+@pytest.mark.parametrize('B', [None, 4, 8])
 def test_pinned_host_images_match_device_tensors(NUFFT, B):
-    """Pinned CPU tensors: the image kernels read and write them in place
-    through their device mapping (no copies); results equal the device-tensor
-    path and the returned tensors are pinned CPU tensors."""
+    """Pinned CPU tensors: for one coil the image kernels read and write them
+    in place through their device mapping (no copies), for several coils they
+    go through copies; results equal the device-tensor path and the returned
+    tensors are pinned CPU tensors."""
     import torch
     rng = np.random.default_rng(41)
     Nd, Kd, Jd = (24, 20, 16), (48, 40, 32), (6, 6, 6)
