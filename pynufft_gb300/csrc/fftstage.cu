@@ -255,6 +255,34 @@ __global__ void pad_cm_rows_kernel(ImgGeom g, const float2* __restrict__ xx, flo
   }
 }
 
+// Several coils, 3D: the Nd corner of every system's zero-kept padded input
+// (its first N0 slabs, `slabsz` = N0 * K1 * K2 cells per system); one block
+// per image row (inst, n0, n1) reads the coil-fastest row once and writes it
+// for every coil.  Cells outside the corner are never written (zero).
+__global__ void pad_cm_corner_kernel(ImgGeom g, const float2* __restrict__ xx,
+                                     float2* __restrict__ pad, int64_t slabsz, int apply_sn,
+                                     int64_t rows) {
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    int64_t inst;
+    int n0, n1;
+    row_index<3>(r, g.N[0], g.N[1], inst, n0, n1);
+    const int NL = g.N[2], B = g.B;
+    const float s_lead = apply_sn ? lead_sn<3>(g.sn[0], g.sn[1], n0, n1) : 1.f;
+    const float2* src = xx + (size_t)r * NL * B;
+    const size_t cell = ((size_t)n0 * g.K[1] + n1) * g.K[2];
+    for (int e = threadIdx.x; e < NL * B; e += blockDim.x) {
+        const int b = e / NL, k = e - b * NL;
+        float2 v = __ldg(src + (size_t)k * B + b);
+        if (apply_sn) {
+            const float sc = s_lead * __ldg(g.sn[2] + k);
+            v.x *= sc;
+            v.y *= sc;
+        }
+        pad[((size_t)inst * B + b) * slabsz + cell + k] = v;
+    }
+  }
+}
+
 // Crop from coil-major spectra: one block per image row writes that row of
 // every coil into the coil-fastest image (x 1/prod(Kd), x sn if apply_sn,
 // / sn if divide_sn).
@@ -471,6 +499,27 @@ int image_from_spectrum_coils(nufft_plan_s* p, const float2* k, float2* xx, bool
 // apply_sn), then the forward FFTs in place.
 int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s) {
     ImgGeom g = img_geom(p);
+    if (p->fft_cm_pruned && p->d_cmpad) {
+        // 3D, a few systems: write only the Nd corners into the zero-kept
+        // padded inputs; per system the (y, z) FFTs of its N0 slabs run out of
+        // place into the zero-kept slab buffer and the x-axis FFTs from there
+        // into the system's coil-major spectrum
+        const int64_t rows = rows_of(g, g.N, p->ninst);
+        const int64_t slabsz = (int64_t)p->Nd[0] * (p->prodK / p->Kd[0]);
+        pad_cm_corner_kernel<<<row_blocks(p, rows), row_threads(g.N[2] * g.B), 0, s>>>(
+            g, xx, p->d_cmpad, slabsz, apply_sn ? 1 : 0, rows);
+        NUFFT_TRY(check_launch("pad_cm_corner_kernel"));
+        NUFFT_CUFFT_TRY(cufftSetStream(p->fft_slab, s));
+        NUFFT_CUFFT_TRY(cufftSetStream(p->fft_x, s));
+        cufftComplex* slab = reinterpret_cast<cufftComplex*>(p->d_cmslab);
+        for (int i = 0; i < p->ninst * p->B; ++i) {
+            cufftComplex* in = reinterpret_cast<cufftComplex*>(p->d_cmpad) + (size_t)i * slabsz;
+            cufftComplex* out = reinterpret_cast<cufftComplex*>(p->d_cm) + (size_t)i * p->prodK;
+            NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_slab, in, slab, CUFFT_FORWARD));
+            NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_x, slab, out, CUFFT_FORWARD));
+        }
+        return NUFFT_OK;
+    }
     const int64_t rows = rows_of(g, g.K, p->ninst);
     const unsigned nb = row_blocks(p, rows);
     const int nt = row_threads(g.K[g.ndim - 1] * g.B);
@@ -679,6 +728,17 @@ int fft_init(nufft_plan_s* p) {
         NUFFT_CUDA_TRY(cudaMalloc(&p->d_fftwork, work));
         p->dev_bytes += work;
     }
+    if (p->fft_cm_pruned) {
+        // per system a padded input (first Nd[0] slabs), one shared slab-FFT
+        // output; both zero once, only their Nd corner / first Nd[0] slabs
+        // are ever written
+        const size_t nin = (size_t)p->ninst * B * p->Nd[0] * (p->prodK / p->Kd[0]);
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_cmpad, sizeof(float2) * nin));
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_cmslab, sizeof(float2) * p->prodK));
+        NUFFT_CUDA_TRY(cudaMemset(p->d_cmpad, 0, sizeof(float2) * nin));
+        NUFFT_CUDA_TRY(cudaMemset(p->d_cmslab, 0, sizeof(float2) * p->prodK));
+        p->dev_bytes += sizeof(float2) * (nin + p->prodK);
+    }
     if (p->fft_pruned) {
         // padded input (first Nd[0] slabs) and slab-FFT output, zero once
         const size_t nin = (size_t)p->Nd[0] * (p->prodK / p->Kd[0]);
@@ -711,7 +771,9 @@ void fft_destroy(nufft_plan_s* p) {
     cudaFree(p->d_padin);
     cudaFree(p->d_slabout);
     cudaFree(p->d_cm);
-    p->d_padin = p->d_slabout = p->d_cm = nullptr;
+    cudaFree(p->d_cmpad);
+    cudaFree(p->d_cmslab);
+    p->d_padin = p->d_slabout = p->d_cm = p->d_cmpad = p->d_cmslab = nullptr;
 }
 
 // direction < 0: forward (numpy fftn sign); > 0: inverse, unnormalised.

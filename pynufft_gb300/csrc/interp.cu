@@ -165,8 +165,11 @@ int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s, b
     // deterministic: exact fixed-point accumulation, then one rounding to float
     if (!p->d_igrid) {
         NUFFT_CUDA_TRY(cudaMalloc(&p->d_igrid, sizeof(unsigned long long) * 2 * ncells));
+        p->dev_bytes += sizeof(unsigned long long) * 2 * ncells;
+    }
+    if (!p->d_dscal) {
         NUFFT_CUDA_TRY(cudaMalloc(&p->d_dscal, sizeof(double) * kScaleSlots));
-        p->dev_bytes += sizeof(unsigned long long) * 2 * ncells + sizeof(double) * kScaleSlots;
+        p->dev_bytes += sizeof(double) * kScaleSlots;
     }
     NUFFT_CUDA_TRY(cudaMemsetAsync(p->d_igrid, 0, sizeof(unsigned long long) * 2 * ncells, s));
     const int64_t ny = p->M * (int64_t)p->B;
@@ -233,10 +236,14 @@ int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_
     // tiles exactly in 64-bit fixed point, then one rounding to float
     if (!p->d_igrid) {
         NUFFT_CUDA_TRY(cudaMalloc(&p->d_igrid, sizeof(unsigned long long) * 2 * ncells));
-        NUFFT_CUDA_TRY(cudaMalloc(&p->d_dscal, sizeof(double) * kScaleSlots));
-        p->dev_bytes += sizeof(unsigned long long) * 2 * ncells + sizeof(double) * kScaleSlots;
+        p->dev_bytes += sizeof(unsigned long long) * 2 * ncells;
     }
-    NUFFT_CUDA_TRY(cudaMemsetAsync(p->d_igrid, 0, sizeof(unsigned long long) * 2 * ncells, s));
+    if (!p->d_dscal) {
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_dscal, sizeof(double) * kScaleSlots));
+        p->dev_bytes += sizeof(double) * kScaleSlots;
+    }
+    unsigned long long* igrid = p->d_igrid;
+    NUFFT_CUDA_TRY(cudaMemsetAsync(igrid, 0, sizeof(unsigned long long) * 2 * ncells, s));
     const int64_t ny = p->M * (int64_t)p->B;
     abs_sum_partial_kernel<<<kAbsSumParts, 256, 0, s>>>(y, ny, p->d_dscal + 2);
     NUFFT_TRY(check_launch("abs_sum_partial_kernel"));
@@ -245,13 +252,13 @@ int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_
     if (p->M > 0) {
         const bool timed = kernel_time_start(p, 1, s);
         const int st = (p->ndim == 2)
-                           ? y2k_cm_dim2(jm, true, g, y, nullptr, p->d_igrid, p->d_dscal, s)
-                           : y2k_cm_dim3(jm, true, g, y, nullptr, p->d_igrid, p->d_dscal, s);
+                           ? y2k_cm_dim2(jm, true, g, y, nullptr, igrid, p->d_dscal, s)
+                           : y2k_cm_dim3(jm, true, g, y, nullptr, igrid, p->d_dscal, s);
         kernel_time_stop(p, 1, s, timed);
         NUFFT_TRY(st);
     }
     const int blocks = (int)std::min<size_t>((ncells + 255) / 256, (size_t)p->num_sms * 16);
-    fixed_to_float_kernel<<<std::max(blocks, 1), 256, 0, s>>>(p->d_igrid, (int64_t)ncells,
+    fixed_to_float_kernel<<<std::max(blocks, 1), 256, 0, s>>>(igrid, (int64_t)ncells,
                                                                p->d_dscal, grid_cm);
     return check_launch("fixed_to_float_kernel");
 }

@@ -198,6 +198,11 @@ struct nufft_plan_s {
     float2* d_pfft_tw = nullptr;      // per-axis, per-stage twiddle tables, concatenated
     int pfft_tw_off[3][4] = {};       // [axis][stage] offsets into d_pfft_tw
     float2* d_cm = nullptr;           // B > 1: coil-major copy of the grid for the FFTs
+    // B > 1 with per-system pruned 3D plans: zero-kept padded inputs (the
+    // first Nd[0] slabs of every system) and slab-FFT outputs (slabs past
+    // Nd[0] stay zero), so the forward writes only the image corner
+    float2* d_cmpad = nullptr;
+    float2* d_cmslab = nullptr;
     size_t dev_bytes = 0;
 
     nufft::Geom geom() const;
