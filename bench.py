@@ -11,7 +11,9 @@ between steps.
 
 Prints ONE JSON line (rank 0).  `value` times steps with inputs resident on
 the device (CUDA events on the launching stream); `e2e` times the public API
-(`NUFFT.forward`/`adjoint` on pinned host tensors, copies included);
+on pinned host tensors, every step's copies in and out included
+(`NUFFT.run_many`, which overlaps one step's copies with the neighbouring
+steps' transforms; `e2e_sync`: `NUFFT.forward`/`adjoint` one call at a time);
 `roofline` uses the dominant kernel's own average duration, from CUDA events
 that the library records around every n-th of its launches (about 20 spread
 over the timed steps) on the launching stream;
@@ -567,30 +569,44 @@ def main():
                            1e-5, 0.0, byref(it), sp)
         cg = {'maxiter': cg_iters, 'iters': it.value, 'ms': t_cg, 'systems': ninst}
 
-    # end to end through the public API, pinned host buffers, copies included
+    # end to end through the public API, pinned host buffers, copies included:
+    # every step copies its image and its samples in and both results out.
+    # `run_many` keeps the host link busy while the GPU transforms (the
+    # copies of one step overlap the neighbouring steps' transforms);
+    # `e2e_sync` calls forward() and adjoint() one at a time, each returning
+    # its host result before the next starts.
     xh = torch.from_numpy(x).pin_memory()
+    yh = A.forward(xh)                   # the steps' sample input (host)
     for _ in range(2):
-        yh = A.forward(xh)
-        A.adjoint(yh)
+        A.adjoint(A.forward(xh))
     torch.cuda.synchronize()
     e2e_steps = max(3, min(args.steps, 50))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        yh = A.forward(xh)
+        yr = A.forward(xh)
         xr = A.adjoint(yh)
+    torch.cuda.synchronize()
+    t_sync = (time.perf_counter() - t0) / e2e_steps / ninst
+    jobs = [j for _ in range(e2e_steps) for j in (('forward', xh), ('adjoint', yh))]
+    outs = [torch.empty_like(xh if name == 'adjoint' else yh).pin_memory() for name, _ in jobs]
+    A.run_many(jobs, out=outs)           # warm-up (streams, device buffers)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    A.run_many(jobs, out=outs)
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / e2e_steps / ninst
     if dist:
-        t = torch.tensor([t_e2e], device=dev)
+        t = torch.tensor([t_e2e, t_sync], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+        t_e2e, t_sync = float(t[0].item()), float(t[1].item())
     h2d = (xh.numel() + yh.numel()) * 8
-    d2h = (yh.numel() + xr.numel()) * 8
+    d2h = (yr.numel() + xr.numel()) * 8
+    del outs
 
     batched = None
     if not args.no_batched and args.config == 'c2':
         A.release()
-        del xd, yd, xo, xh, yh, xr
+        del xd, yd, xo, xh, yh, xr, yr
         if scratch is not None:
             del scratch
         torch.cuda.empty_cache()
@@ -617,7 +633,9 @@ def main():
                        'frac': nbytes / (t_k2y / 1e3) / 1e9 / peak},
             'cpu_baseline': cpu,
             'e2e': {'value': world / t_e2e, 'unit': 'pairs/s', 'h2d_bytes_per_step': h2d,
-                    'd2h_bytes_per_step': d2h},
+                    'd2h_bytes_per_step': d2h, 'api': 'NUFFT.run_many', 'steps': e2e_steps},
+            'e2e_sync': {'value': world / t_sync, 'unit': 'pairs/s',
+                         'api': 'NUFFT.forward + NUFFT.adjoint, one call at a time'},
             'gpu_launches': launches_per_step * args.steps,
             'plan_ms': plan_ms,
             'cg': cg,

@@ -392,6 +392,101 @@ class NUFFT:
     def k2y2k(self, k):
         return self._call(self._lib.nufft_k2y2k, k, 'k', 'k', 'k2y2k')
 
+    # ---- many host arrays, copies overlapped with the transforms
+    _STAGES = {'forward': ('x', 'y'), 'adjoint': ('y', 'x'), 'selfadjoint': ('x', 'x'),
+               'x2xx': ('x', 'x'), 'xx2x': ('x', 'x'), 'xx2k': ('x', 'k'), 'k2xx': ('k', 'x'),
+               'k2y': ('k', 'y'), 'y2k': ('y', 'k'), 'k2y2k': ('k', 'k')}
+
+    def run_many(self, jobs, depth=2, out=None):
+        """Apply a sequence of operators to host arrays, with the host link
+        busy while the GPU transforms.
+
+        jobs: iterable of (name, array): name one of forward, adjoint,
+        selfadjoint, x2xx, xx2x, xx2k, k2xx, k2y, y2k, k2y2k; array a CPU
+        tensor or numpy array of that operator's input shape (pinned CPU
+        tensors are copied without staging).  Inputs are copied to the
+        device on an upload stream, the operators run in order on the
+        current stream, and results are copied back on a download stream
+        into pinned CPU tensors, so the copies of job i+1's input and job
+        i-1's result overlap job i's transform; `depth` jobs' device buffers
+        rotate.  Returns the results in order (written into `out`, a list of
+        pinned complex64 CPU tensors of the results' shapes, when given).
+        Each result equals that of calling the method alone.
+        """
+        torch = _torch()
+        if self._plan is None:
+            raise RuntimeError('plan() has not been called')
+        if depth < 1:
+            raise ValueError('depth must be at least 1')
+        todo = []
+        for name, a in jobs:
+            if name not in self._STAGES:
+                raise ValueError(f'unknown operator {name!r}')
+            kin, kout = self._STAGES[name]
+            if isinstance(a, torch.Tensor):
+                if a.is_cuda:
+                    raise ValueError('run_many takes host arrays; call the method on device tensors')
+                h = a.to(torch.complex64).contiguous()
+            else:
+                h = torch.from_numpy(numpy.ascontiguousarray(a, dtype=numpy.complex64))
+            if tuple(h.shape) != self._shape(kin):
+                raise ValueError(f'{name}: expected shape {self._shape(kin)}, got {tuple(h.shape)}')
+            todo.append((name, h if h.is_pinned() else h.pin_memory(), kin, kout))
+        if out is not None:
+            out = list(out)
+            if len(out) != len(todo):
+                raise ValueError(f'out: {len(out)} tensors for {len(todo)} jobs')
+            for (name, _, _, kout), o in zip(todo, out):
+                if (not isinstance(o, torch.Tensor) or o.is_cuda or not o.is_pinned()
+                        or o.dtype != torch.complex64 or not o.is_contiguous()
+                        or tuple(o.shape) != self._shape(kout)):
+                    raise ValueError(f'out: {name} needs a pinned contiguous complex64 CPU '
+                                     f'tensor of shape {self._shape(kout)}')
+        dev = self.device
+        comp = torch.cuda.current_stream(dev)
+        up = torch.cuda.Stream(dev)
+        down = torch.cuda.Stream(dev)
+        bufs = {}
+        freed_in = [None] * depth     # compute of the slot's last job done
+        freed_out = [None] * depth    # download of the slot's last result done
+        outs = []
+        with torch.cuda.device(dev):
+            for i, (name, h, kin, kout) in enumerate(todo):
+                s = i % depth
+                din = bufs.get((s, 'in', kin))
+                if din is None:
+                    din = bufs[(s, 'in', kin)] = self._empty(kin)
+                dout = bufs.get((s, 'out', kout))
+                if dout is None:
+                    dout = bufs[(s, 'out', kout)] = self._empty(kout)
+                with torch.cuda.stream(up):
+                    if freed_in[s] is not None:
+                        up.wait_event(freed_in[s])
+                    din.copy_(h, non_blocking=True)
+                    ev_up = torch.cuda.Event()
+                    ev_up.record(up)
+                comp.wait_event(ev_up)
+                if freed_out[s] is not None:
+                    comp.wait_event(freed_out[s])
+                fn = getattr(self._lib, 'nufft_' + name)
+                _lib.check(fn(self._plan, c_void_p(din.data_ptr()), c_void_p(dout.data_ptr()),
+                              c_void_p(comp.cuda_stream)), name)
+                ev_comp = torch.cuda.Event()
+                ev_comp.record(comp)
+                freed_in[s] = ev_comp
+                o = (out[i] if out is not None else
+                     torch.empty(self._shape(kout), dtype=torch.complex64, pin_memory=True))
+                with torch.cuda.stream(down):
+                    down.wait_event(ev_comp)
+                    o.copy_(dout, non_blocking=True)
+                    ev_down = torch.cuda.Event()
+                    ev_down.record(down)
+                freed_out[s] = ev_down
+                outs.append(o)
+            down.synchronize()
+            comp.wait_stream(up)      # the buffers die with this call
+        return outs
+
     # ---- single-image FFT stages (nufft/_nufft_class_methods_cpu.py:251-264, 332-344)
     def _single_image_plan(self):
         """This plan when it is one coil and one instance; otherwise a
