@@ -345,6 +345,30 @@ def batched_leg(torch, dev, peak, steps):
         lib.nufft_plan_kernel_timing(A._plan, 0)
         t_k2y = k_ms.value / max(k_n.value, 1)
         t_y2k = y_ms.value / max(y_n.value, 1)
+        # solve(y, 'cg') on every coil (one system each): 15 iterations for
+        # the 2D radial workload, 10 for the kooshball; and the kooshball's
+        # trajectory derivative (d forward / d om, every axis and coil)
+        cg_iters = 15 if cfg == 'c3' else 10
+        xcg = torch.empty_like(xd)
+        it = c_int(0)
+
+        def solve():
+            lib.nufft_solve_cg(A._plan, c_void_p(yd.data_ptr()), c_void_p(xcg.data_ptr()), cg_iters,
+                               1e-5, 0.0, None, sp)
+        ms_cg = time_pairs(torch, stream, solve, 3, warmup=1)
+        lib.nufft_solve_cg(A._plan, c_void_p(yd.data_ptr()), c_void_p(xcg.data_ptr()), cg_iters,
+                           1e-5, 0.0, byref(it), sp)
+        cg = {'maxiter': cg_iters, 'iters': it.value, 'ms': ms_cg, 'systems': B}
+        del xcg
+        dom = None
+        if cfg == 'c5':
+            dy = torch.empty((len(c['Nd']), M, B), dtype=torch.complex64, device=dev)
+
+            def fdom():
+                lib.nufft_forward_dom(A._plan, c_void_p(xd.data_ptr()), c_void_p(dy.data_ptr()), sp)
+            dom = {'ms': time_pairs(torch, stream, fdom, 3, warmup=1),
+                   'what': 'd forward / d om for every axis and coil (nufft_forward_dom)'}
+            del dy
         A.release()
         del yd, xo
         # the plain path: one single-coil plan, the coils' pairs one after another
@@ -376,6 +400,8 @@ def batched_leg(torch, dev, peak, steps):
                       'how': f'{B} single-coil forward+adjoint pairs in turn through one '
                              'single-coil plan of the same points'},
             'speedup_vs_plain': ms_p / ms_b,
+            'cg': cg,
+            'forward_dom': dom,
             'steps': steps,
         }
     return out

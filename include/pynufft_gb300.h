@@ -227,7 +227,7 @@ int nufft_set_sense(nufft_plan_t plan, const void* maps, int maps_on_device, voi
 int nufft_forward_one2many(nufft_plan_t plan, const void* x, void* y, void* stream);
 int nufft_adjoint_many2one(nufft_plan_t plan, const void* y, void* x, void* stream);
 
-/* Gridding (y2k) with the exact 64-bit fixed-point accumulation of the
+/* Gridding (y2k) with the 64-bit fixed-point accumulation of the
  * deterministic mode, for callers that cannot allocate device memory while
  * they run: applications that hand all GPU memory to their own pool up front
  * (where a stray cudaMalloc can fail or fragment the pool) and
@@ -242,7 +242,11 @@ int nufft_adjoint_many2one(nufft_plan_t plan, const void* y, void* x, void* stre
  * capture.  All calls share the scratch, which keeps the last call's
  * contents (each call clears it first): calls that overlap on the GPU, on
  * different streams or threads, race.  Works on any plan; the result equals
- * nufft_y2k on a plan created with NUFFT_FLAG_DETERMINISTIC. */
+ * nufft_y2k on a plan created with NUFFT_FLAG_DETERMINISTIC, bit for bit:
+ * every contribution summed exactly, or, on plans of 8 or more coils that
+ * grid by tile rows, per-row float sums in a fixed order combined exactly
+ * (those plans also use their coil-major spectrum buffer, allocated with the
+ * plan, before one transpose into k). */
 #define NUFFT_STATIC_SCRATCH_CELLS (1u << 20)
 int nufft_y2k_exact_static(nufft_plan_t plan, const void* y, void* k, void* stream);
 

@@ -411,7 +411,7 @@ int nufft_k2y(nufft_plan_t p, const void* k, void* y, void* stream) {
 int nufft_y2k(nufft_plan_t p, const void* y, void* k, void* stream) {
     NUFFT_TRY(need_points(p, "nufft_y2k"));
     NUFFT_TRY(need_ptrs(y, k, "nufft_y2k", p));
-    return launch_y2k(p, (const float2*)y, (float2*)k, as_stream(stream));
+    return launch_y2k_grid(p, (const float2*)y, (float2*)k, as_stream(stream));
 }
 
 static bool capturing(cudaStream_t s) {
@@ -473,7 +473,7 @@ int nufft_k2y2k(nufft_plan_t p, const void* k, void* k_out, void* stream) {
     NUFFT_TRY(need_ptrs(k, k_out, "nufft_k2y2k"));
     cudaStream_t s = as_stream(stream);
     NUFFT_TRY(launch_k2y(p, (const float2*)k, p->d_ybuf, s));
-    return launch_y2k(p, p->d_ybuf, (float2*)k_out, s);
+    return launch_y2k_grid(p, p->d_ybuf, (float2*)k_out, s);
 }
 
 int nufft_solve_cg(nufft_plan_t p, const void* y, void* x, int maxiter, double rtol, double atol,
@@ -554,8 +554,9 @@ int nufft_forward_dom(nufft_plan_t p, const void* x, void* dy, void* stream) {
     cudaStream_t s = as_stream(stream);
     const size_t stride = (size_t)p->M * p->B;
     for (int d = 0; d < p->ndim; ++d) {
-        NUFFT_TRY(launch_pad(p, (const float2*)x, p->d_grid, true, d, s));
-        NUFFT_TRY(fft_exec(p, p->d_grid, -1, s));
+        // the forward's own path (several coils: coil-major, pruned FFTs)
+        // with the image also multiplied by -i (n_d - N_d/2)
+        NUFFT_TRY(forward_from_image(p, (const float2*)x, true, p->d_grid, s, d));
         NUFFT_TRY(launch_k2y(p, p->d_grid, (float2*)dy + d * stride, s));
     }
     return NUFFT_OK;

@@ -272,7 +272,7 @@ static int issue_init(nufft_plan_s* p, const CGGeom& g, const float2* y, int max
     double2* part = reinterpret_cast<double2*>(p->d_part);
     const dim3 rgrid(g.nblk, g.ninst);
     NUFFT_CUDA_TRY(cudaMemsetAsync(xk, 0, sizeof(float2) * n, s));
-    NUFFT_TRY(launch_y2k(p, y, r, s));
+    NUFFT_TRY(launch_y2k_grid(p, y, r, s));
     cg_norm_kernel<<<rgrid, g.B * g.Q, 0, s>>>(g, r, part);
     NUFFT_TRY(check_launch("cg_norm_kernel"));
     cg_init_sys_kernel<<<g.S, kSumThreads, 0, s>>>(g, part, sys, rtol, atol, maxiter);
@@ -294,7 +294,7 @@ static int issue_iters(nufft_plan_s* p, const CGGeom& g, int iters, cudaStream_t
         cg_update_p_kernel<<<rgrid, rthreads, 0, s>>>(g, sys, r, pv);
         NUFFT_TRY(check_launch("cg_update_p_kernel"));
         NUFFT_TRY(launch_k2y(p, pv, p->d_ybuf, s));          // q = spH sp p
-        NUFFT_TRY(launch_y2k(p, p->d_ybuf, q, s));
+        NUFFT_TRY(launch_y2k_grid(p, p->d_ybuf, q, s));
         cg_dot_kernel<<<rgrid, rthreads, 0, s>>>(g, pv, q, part);
         NUFFT_TRY(check_launch("cg_dot_kernel"));
         cg_alpha_kernel<<<g.S, kSumThreads, 0, s>>>(g, part, sys);
@@ -355,7 +355,7 @@ int solve_cg(nufft_plan_s* p, const float2* y, float2* x, int maxiter, double rt
         p->cg_rtol != rtol || p->cg_atol != atol || !p->cg_iter_exec || p->cg_chunk != chunk) {
         // one uncaptured gridding pass first: it creates any lazily allocated
         // buffers and sets kernel attributes outside the capture
-        NUFFT_TRY(launch_y2k(p, p->d_ybuf, p->d_grid, s));
+        NUFFT_TRY(launch_y2k_grid(p, p->d_ybuf, p->d_grid, s));
         NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
         NUFFT_TRY(capture(&p->cg_init_exec, [&](cudaStream_t cs) {
             return issue_init(p, g, y, maxiter, rtol, atol, cs);

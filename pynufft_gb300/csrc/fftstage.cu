@@ -220,7 +220,7 @@ __global__ void crop_rows_kernel(ImgGeom g, const float2* __restrict__ grid, flo
 // the Nd corner), reading the coil-fastest image row once through L1.
 template <int DIM>
 __global__ void pad_cm_rows_kernel(ImgGeom g, const float2* __restrict__ xx, float2* __restrict__ cm,
-                                   int apply_sn, int64_t rows) {
+                                   int apply_sn, int dom_axis, int64_t rows) {
   for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
     int64_t inst;
     int n[3] = {0, 0, 0};
@@ -238,6 +238,9 @@ __global__ void pad_cm_rows_kernel(ImgGeom g, const float2* __restrict__ xx, flo
         xrow = xrow * g.N[d] + n[d];
     }
     const float s_lead = (apply_sn && inside) ? lead_sn<DIM>(g.sn[0], g.sn[1], n[0], n[1]) : 1.f;
+    float a_lead = 0.f;
+    if (DIM >= 2 && dom_axis == 0) a_lead = (float)n[0] - 0.5f * (float)g.N[0];
+    if (DIM == 3 && dom_axis == 1) a_lead = (float)n[1] - 0.5f * (float)g.N[1];
     const float2* src = xx + (size_t)xrow * NL * B;
     for (int e = threadIdx.x; e < KL * B; e += blockDim.x) {
         const int b = e / KL, k = e - b * KL;
@@ -248,6 +251,10 @@ __global__ void pad_cm_rows_kernel(ImgGeom g, const float2* __restrict__ xx, flo
                 const float sc = s_lead * __ldg(g.sn[last] + k);
                 v.x *= sc;
                 v.y *= sc;
+            }
+            if (dom_axis >= 0) {   // x -i (n_a - N_a/2): the trajectory derivative
+                const float a = (dom_axis == last) ? (float)k - 0.5f * (float)NL : a_lead;
+                v = make_float2(a * v.y, -a * v.x);
             }
         }
         cm[((size_t)inst * B + b) * g.prodK + (size_t)klocal * KL + k] = v;
@@ -261,13 +268,15 @@ __global__ void pad_cm_rows_kernel(ImgGeom g, const float2* __restrict__ xx, flo
 // for every coil.  Cells outside the corner are never written (zero).
 __global__ void pad_cm_corner_kernel(ImgGeom g, const float2* __restrict__ xx,
                                      float2* __restrict__ pad, int64_t slabsz, int apply_sn,
-                                     int64_t rows) {
+                                     int dom_axis, int64_t rows) {
   for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
     int64_t inst;
     int n0, n1;
     row_index<3>(r, g.N[0], g.N[1], inst, n0, n1);
     const int NL = g.N[2], B = g.B;
     const float s_lead = apply_sn ? lead_sn<3>(g.sn[0], g.sn[1], n0, n1) : 1.f;
+    const float a_lead = (dom_axis == 0) ? (float)n0 - 0.5f * (float)g.N[0]
+                         : (dom_axis == 1) ? (float)n1 - 0.5f * (float)g.N[1] : 0.f;
     const float2* src = xx + (size_t)r * NL * B;
     const size_t cell = ((size_t)n0 * g.K[1] + n1) * g.K[2];
     for (int e = threadIdx.x; e < NL * B; e += blockDim.x) {
@@ -277,6 +286,10 @@ __global__ void pad_cm_corner_kernel(ImgGeom g, const float2* __restrict__ xx,
             const float sc = s_lead * __ldg(g.sn[2] + k);
             v.x *= sc;
             v.y *= sc;
+        }
+        if (dom_axis >= 0) {   // x -i (n_a - N_a/2): the trajectory derivative
+            const float a = (dom_axis == 2) ? (float)k - 0.5f * (float)NL : a_lead;
+            v = make_float2(a * v.y, -a * v.x);
         }
         pad[((size_t)inst * B + b) * slabsz + cell + k] = v;
     }
@@ -494,10 +507,14 @@ int image_from_spectrum_coils(nufft_plan_s* p, const float2* k, float2* xx, bool
     return cm_to_image(p, xx, apply_sn, divide_sn, s);
 }
 
+int cm_to_grid(const nufft_plan_s* p, float2* k, cudaStream_t s) {
+    return coil_transpose(p, p->d_cm, k, false, s);
+}
+
 // Several coils: image xx (coil-fastest) -> coil-major spectra in p->d_cm:
 // every coil's grid padded straight into the coil-major buffer (x sn when
 // apply_sn), then the forward FFTs in place.
-int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s) {
+int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s, int dom_axis) {
     ImgGeom g = img_geom(p);
     if (p->fft_cm_pruned && p->d_cmpad) {
         // 3D, a few systems: write only the Nd corners into the zero-kept
@@ -507,7 +524,7 @@ int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s
         const int64_t rows = rows_of(g, g.N, p->ninst);
         const int64_t slabsz = (int64_t)p->Nd[0] * (p->prodK / p->Kd[0]);
         pad_cm_corner_kernel<<<row_blocks(p, rows), row_threads(g.N[2] * g.B), 0, s>>>(
-            g, xx, p->d_cmpad, slabsz, apply_sn ? 1 : 0, rows);
+            g, xx, p->d_cmpad, slabsz, apply_sn ? 1 : 0, dom_axis, rows);
         NUFFT_TRY(check_launch("pad_cm_corner_kernel"));
         NUFFT_CUFFT_TRY(cufftSetStream(p->fft_slab, s));
         NUFFT_CUFFT_TRY(cufftSetStream(p->fft_x, s));
@@ -525,9 +542,9 @@ int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s
     const int nt = row_threads(g.K[g.ndim - 1] * g.B);
     const int as = apply_sn ? 1 : 0;
     switch (p->ndim) {
-        case 1: pad_cm_rows_kernel<1><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, rows); break;
-        case 2: pad_cm_rows_kernel<2><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, rows); break;
-        default: pad_cm_rows_kernel<3><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, rows); break;
+        case 1: pad_cm_rows_kernel<1><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, dom_axis, rows); break;
+        case 2: pad_cm_rows_kernel<2><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, dom_axis, rows); break;
+        default: pad_cm_rows_kernel<3><<<nb, nt, 0, s>>>(g, xx, p->d_cm, as, dom_axis, rows); break;
     }
     NUFFT_TRY(check_launch("pad_cm_rows_kernel"));
     return fft_cm_exec(p, -1, s);
@@ -541,11 +558,15 @@ int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s
 // FFTs write k: the 134 MB zero fill of a 256^3 grid is not rewritten on
 // every call.
 int forward_from_image(nufft_plan_s* p, const float2* xx, bool apply_sn, float2* k,
-                       cudaStream_t s) {
+                       cudaStream_t s, int dom_axis) {
     if (p->B > 1) {
         // coil-major: pad every coil's grid, transform there, transpose to k
-        NUFFT_TRY(image_to_cm(p, xx, apply_sn, s));
+        NUFFT_TRY(image_to_cm(p, xx, apply_sn, s, dom_axis));
         return coil_transpose(p, p->d_cm, k, false, s);
+    }
+    if (dom_axis >= 0) {
+        NUFFT_TRY(launch_pad(p, xx, k, apply_sn, dom_axis, s));
+        return fft_exec(p, k, -1, s);
     }
     if (p->pfft) return pfft_forward(p, xx, apply_sn, k, s);
     if (!(p->fft_pruned && p->d_padin)) {

@@ -219,11 +219,41 @@ bool cm_path(const nufft_plan_s* p) {
     return nkey <= 256 && rows_smem(p->ndim, J, nkey, kRowSub, 8) <= 200 * 1024;
 }
 
-int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s) {
+// Deterministic row gridding into the coil-major spectra grid_cm: per-row
+// float sums in a fixed order, combined across tiles exactly in 64-bit fixed
+// point (igrid: 2 * ninst * prodK * B accumulators), then one rounding to
+// float; dscal holds kScaleSlots doubles.  Allocates nothing.  `timer`: the
+// plan whose kernel timing covers the launch, or null.
+static int y2k_cm_det(const nufft_plan_s* p, const float2* y, float2* grid_cm,
+                      unsigned long long* igrid, double* dscal, nufft_plan_s* timer,
+                      cudaStream_t s) {
     const size_t ncells = (size_t)p->ninst * p->prodK * p->B;
     Geom g = p->geom();
-    const int jm = pick_jm(p);
+    NUFFT_CUDA_TRY(cudaMemsetAsync(igrid, 0, sizeof(unsigned long long) * 2 * ncells, s));
+    const int64_t ny = p->M * (int64_t)p->B;
+    abs_sum_partial_kernel<<<kAbsSumParts, 256, 0, s>>>(y, ny, dscal + 2);
+    NUFFT_TRY(check_launch("abs_sum_partial_kernel"));
+    fixed_scale_kernel<<<1, 256, 0, s>>>(dscal + 2, kAbsSumParts, p->wmax, dscal);
+    NUFFT_TRY(check_launch("fixed_scale_kernel"));
+    if (p->M > 0) {
+        const int jm = pick_jm(p);
+        const bool timed = timer && kernel_time_start(timer, 1, s);
+        const int st = (p->ndim == 2) ? y2k_cm_dim2(jm, true, g, y, nullptr, igrid, dscal, s)
+                                      : y2k_cm_dim3(jm, true, g, y, nullptr, igrid, dscal, s);
+        if (timer) kernel_time_stop(timer, 1, s, timed);
+        NUFFT_TRY(st);
+    }
+    const int blocks = (int)std::min<size_t>((ncells + 255) / 256, (size_t)p->num_sms * 16);
+    fixed_to_float_kernel<<<std::max(blocks, 1), 256, 0, s>>>(igrid, (int64_t)ncells, dscal,
+                                                               grid_cm);
+    return check_launch("fixed_to_float_kernel");
+}
+
+int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s) {
+    const size_t ncells = (size_t)p->ninst * p->prodK * p->B;
     if (!(p->flags & NUFFT_FLAG_DETERMINISTIC)) {
+        Geom g = p->geom();
+        const int jm = pick_jm(p);
         NUFFT_CUDA_TRY(cudaMemsetAsync(grid_cm, 0, sizeof(float2) * ncells, s));
         if (p->M == 0) return NUFFT_OK;
         const bool timed = kernel_time_start(p, 1, s);
@@ -232,8 +262,6 @@ int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_
         kernel_time_stop(p, 1, s, timed);
         return st;
     }
-    // deterministic: per-row float sums in a fixed order, combined across
-    // tiles exactly in 64-bit fixed point, then one rounding to float
     if (!p->d_igrid) {
         NUFFT_CUDA_TRY(cudaMalloc(&p->d_igrid, sizeof(unsigned long long) * 2 * ncells));
         p->dev_bytes += sizeof(unsigned long long) * 2 * ncells;
@@ -242,25 +270,19 @@ int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_
         NUFFT_CUDA_TRY(cudaMalloc(&p->d_dscal, sizeof(double) * kScaleSlots));
         p->dev_bytes += sizeof(double) * kScaleSlots;
     }
-    unsigned long long* igrid = p->d_igrid;
-    NUFFT_CUDA_TRY(cudaMemsetAsync(igrid, 0, sizeof(unsigned long long) * 2 * ncells, s));
-    const int64_t ny = p->M * (int64_t)p->B;
-    abs_sum_partial_kernel<<<kAbsSumParts, 256, 0, s>>>(y, ny, p->d_dscal + 2);
-    NUFFT_TRY(check_launch("abs_sum_partial_kernel"));
-    fixed_scale_kernel<<<1, 256, 0, s>>>(p->d_dscal + 2, kAbsSumParts, p->wmax, p->d_dscal);
-    NUFFT_TRY(check_launch("fixed_scale_kernel"));
-    if (p->M > 0) {
-        const bool timed = kernel_time_start(p, 1, s);
-        const int st = (p->ndim == 2)
-                           ? y2k_cm_dim2(jm, true, g, y, nullptr, igrid, p->d_dscal, s)
-                           : y2k_cm_dim3(jm, true, g, y, nullptr, igrid, p->d_dscal, s);
-        kernel_time_stop(p, 1, s, timed);
-        NUFFT_TRY(st);
+    return y2k_cm_det(p, y, grid_cm, p->d_igrid, p->d_dscal, p, s);
+}
+
+// The y2k stage into the caller's coil-fastest spectrum k.  Deterministic
+// plans with the row kernels grid coil-major and transpose once (the 8-coil,
+// 8M-point kooshball: 19 ms against 111 ms for the coil-team kernel's
+// per-contribution 64-bit atomics); the others run launch_y2k.
+int launch_y2k_grid(nufft_plan_s* p, const float2* y, float2* k, cudaStream_t s) {
+    if ((p->flags & NUFFT_FLAG_DETERMINISTIC) && cm_path(p)) {
+        NUFFT_TRY(launch_y2k_cm(p, y, p->d_cm, s));
+        return cm_to_grid(p, k, s);
     }
-    const int blocks = (int)std::min<size_t>((ncells + 255) / 256, (size_t)p->num_sms * 16);
-    fixed_to_float_kernel<<<std::max(blocks, 1), 256, 0, s>>>(igrid, (int64_t)ncells,
-                                                               p->d_dscal, grid_cm);
-    return check_launch("fixed_to_float_kernel");
+    return launch_y2k(p, y, k, s);
 }
 
 // Exact (fixed-point) gridding into `grid` using caller-provided scratch:
@@ -268,6 +290,12 @@ int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_
 // Allocates nothing.
 int launch_y2k_exact_into(const nufft_plan_s* p, const float2* y, float2* grid,
                           unsigned long long* acc, double* scal, cudaStream_t s) {
+    if (cm_path(p)) {
+        // plans with the row kernels: the deterministic stage's own path
+        // (launch_y2k_grid), into the plan's coil-major buffer and one transpose
+        NUFFT_TRY(y2k_cm_det(p, y, p->d_cm, acc, scal, nullptr, s));
+        return cm_to_grid(p, grid, s);
+    }
     const size_t ncells = (size_t)p->ninst * p->prodK * p->B;
     Geom g = p->geom();
     g.ymethod = (p->B >= 8) ? NUFFT_Y2K_COIL : NUFFT_Y2K_ZTEAM;

@@ -262,6 +262,9 @@ int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s,
 // plan's geometry has the row kernels, and y2k into the p->d_cm layout
 bool cm_path(const nufft_plan_s* p);
 int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s);
+// the y2k stage into a coil-fastest spectrum (the row kernels and one
+// transpose for deterministic plans that have them, else launch_y2k)
+int launch_y2k_grid(nufft_plan_s* p, const float2* y, float2* k, cudaStream_t s);
 
 // fftstage.cu
 int launch_scale(const nufft_plan_s* p, const float2* in, float2* out, cudaStream_t s);
@@ -270,13 +273,18 @@ int launch_pad(const nufft_plan_s* p, const float2* xx, float2* grid, bool apply
 int launch_crop(const nufft_plan_s* p, const float2* grid, float2* xx, bool apply_sn,
                 bool divide_sn, cudaStream_t s);
 int fft_exec(nufft_plan_s* p, float2* grid, int direction, cudaStream_t s);
+// dom_axis >= 0: the image is also multiplied by -i (n_a - N_a/2) along that
+// axis (the trajectory derivative)
 int forward_from_image(nufft_plan_s* p, const float2* xx, bool apply_sn, float2* k,
-                       cudaStream_t s);
+                       cudaStream_t s, int dom_axis = -1);
 int image_from_spectrum_coils(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn,
                               bool divide_sn, cudaStream_t s);
 // several coils, coil-major spectra in p->d_cm: image -> spectra / spectra -> image
-int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s);
+int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s,
+                int dom_axis = -1);
 int cm_to_image(nufft_plan_s* p, float2* xx, bool apply_sn, bool divide_sn, cudaStream_t s);
+// the coil-major spectra in p->d_cm -> coil-fastest spectrum k (one transpose)
+int cm_to_grid(const nufft_plan_s* p, float2* k, cudaStream_t s);
 int launch_pad_sense(const nufft_plan_s* p, const float2* x, float2* grid, cudaStream_t s);
 int launch_crop_sense(const nufft_plan_s* p, const float2* grid, float2* x, cudaStream_t s);
 int fft_init(nufft_plan_s* p);

@@ -18,6 +18,8 @@
 //   5. subproblems     : bins split into chunks of <= maxsub points
 #include "nufft_internal.cuh"
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include <cmath>
 #include <algorithm>
 #include <cstring>
@@ -108,6 +110,41 @@ __global__ void bin_points_kernel(const double* __restrict__ om, int64_t M, int 
         }
         bin_of[m] = (int)(bin * 32 + key);
         rank_of[m] = atomicAdd(&bucket_count[bin * 32 + key], 1);
+    }
+}
+
+// Deterministic ranks.  The counter of bin_points_kernel ranks a bucket's
+// points (bin, bank key) in the order threads reach it, which changes from
+// run to run; the tables would then order a bin's points differently on
+// every plan, and so would the row gridding's fixed-order float sums.
+// Instead: the bucket ids sorted stably (a radix sort, the point indices as
+// values), and rank = position - the bucket's first position, i.e. the
+// number of points of lower index in the bucket.  Invalid points (bin -1)
+// take the extra bucket nb32 and no rank.
+__global__ void rank_keys_kernel(const int* __restrict__ bin_of, int64_t M, unsigned nb32,
+                                 unsigned* __restrict__ keys, int* __restrict__ idx) {
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
+         m += (int64_t)gridDim.x * blockDim.x) {
+        const int b = bin_of[m];
+        keys[m] = (b < 0) ? nb32 : (unsigned)b;
+        idx[m] = (int)m;
+    }
+}
+
+__global__ void bucket_head_kernel(const unsigned* __restrict__ keys, int64_t M,
+                                   int* __restrict__ head) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < M;
+         i += (int64_t)gridDim.x * blockDim.x)
+        if (i == 0 || keys[i] != keys[i - 1]) head[keys[i]] = (int)i;
+}
+
+__global__ void sorted_rank_kernel(const unsigned* __restrict__ keys, const int* __restrict__ idx,
+                                   int64_t M, unsigned nb32, const int* __restrict__ head,
+                                   int* __restrict__ rank_of) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < M;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned k = keys[i];
+        if (k < nb32) rank_of[idx[i]] = (int)i - head[k];
     }
 }
 
@@ -552,6 +589,9 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     int *d_gnsub = nullptr, *d_gsubst = nullptr, *d_rnl = nullptr, *d_rst = nullptr;
     int* d_slot = nullptr;
     unsigned int* d_wmax = nullptr;
+    unsigned *d_key = nullptr, *d_key2 = nullptr;
+    int *d_idx = nullptr, *d_idx2 = nullptr, *d_head = nullptr;
+    void* d_sort_tmp = nullptr;
     AxisTab* d_tab = nullptr;
     double* d_ctab = nullptr;
     auto cleanup = [&]() {
@@ -562,6 +602,11 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
         cudaFree(d_nsub); cudaFree(d_subst); cudaFree(d_err); cudaFree(d_wmax);
         cudaFree(d_gnsub); cudaFree(d_gsubst); cudaFree(d_rnl); cudaFree(d_rst);
         cudaFree(d_bucket); cudaFree(d_slot);
+        cudaFree(d_key); cudaFree(d_key2); cudaFree(d_idx); cudaFree(d_idx2); cudaFree(d_head);
+        cudaFree(d_sort_tmp);
+        d_key = d_key2 = nullptr;
+        d_idx = d_idx2 = d_head = nullptr;
+        d_sort_tmp = nullptr;
     };
 #define TRY_TMP(expr)                                                              \
     do {                                                                           \
@@ -627,6 +672,27 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
     if (M > 0) {
         bin_points_kernel<<<blocks, threads, 0, s>>>(d_om, M, nd, p->d_axc, g, d_bin_of, d_rank,
                                                      d_bucket, d_err);
+        TRY_TMP(cudaGetLastError());
+        // ranks by point index (see rank_keys_kernel)
+        const unsigned nb32 = (unsigned)(nbins * 32);
+        int nbits = 1;
+        while (nbits < 32 && (1ull << nbits) <= (unsigned long long)nb32) ++nbits;
+        TRY_TMP(cudaMalloc(&d_key, sizeof(unsigned) * M));
+        TRY_TMP(cudaMalloc(&d_key2, sizeof(unsigned) * M));
+        TRY_TMP(cudaMalloc(&d_idx, sizeof(int) * M));
+        TRY_TMP(cudaMalloc(&d_idx2, sizeof(int) * M));
+        TRY_TMP(cudaMalloc(&d_head, sizeof(int) * ((size_t)nb32 + 1)));
+        rank_keys_kernel<<<blocks, threads, 0, s>>>(d_bin_of, M, nb32, d_key, d_idx);
+        TRY_TMP(cudaGetLastError());
+        size_t tmp_bytes = 0;
+        TRY_TMP(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, d_key, d_key2, d_idx, d_idx2,
+                                                M, 0, nbits, s));
+        TRY_TMP(cudaMalloc(&d_sort_tmp, std::max<size_t>(tmp_bytes, 16)));
+        TRY_TMP(cub::DeviceRadixSort::SortPairs(d_sort_tmp, tmp_bytes, d_key, d_key2, d_idx, d_idx2,
+                                                M, 0, nbits, s));
+        bucket_head_kernel<<<blocks, threads, 0, s>>>(d_key2, M, d_head);
+        TRY_TMP(cudaGetLastError());
+        sorted_rank_kernel<<<blocks, threads, 0, s>>>(d_key2, d_idx2, M, nb32, d_head, d_rank);
         TRY_TMP(cudaGetLastError());
     }
     {

@@ -6,7 +6,7 @@ of 32 coils gridding by register rows straight into coil-major spectra
 batch semantics) at 1e-5 relative L2, for 2D and 3D, J in {4, 6, 8}, 8 to 32
 coils, one or several instances, clustered points (bins split into several
 sub-problems), both gridding modes; the deterministic mode bitwise
-repeatable."""
+repeatable, on one plan and across plans of the same points."""
 import numpy as np
 import pytest
 
@@ -77,3 +77,28 @@ def test_coil_major_many_instances_match_oracle(ndim, B):
         assert rel_l2(yf[sl], O.forward(x[i])) < TOL, i
         assert rel_l2(xa[i], O.adjoint(y[sl])) < TOL, i
         off += Ms[i]
+
+
+@pytest.mark.parametrize('Nd,Kd,J,B', [((12, 14, 10), (24, 28, 20), 6, 8),
+                                       ((24, 20), (48, 40), 6, 32),
+                                       ((24, 20), (48, 40), 6, None)])
+def test_deterministic_plans_of_the_same_points_agree_bitwise(Nd, Kd, J, B):
+    """Two deterministic plans of the same points (planned separately, so
+    their binning ran twice) give bitwise equal adjoints, y2k stages and
+    10-iteration CG solves: a bin's points are ranked by index, not in the
+    order threads reached the bin, so the row gridding's fixed-order float
+    sums are the same on every plan."""
+    from pynufft_gb300 import NUFFT
+    rng = np.random.default_rng(82)
+    M = 4000
+    om = _points(rng, M, len(Nd))
+    y = cplx(rng, (M,) + (() if B is None else (B,)))
+    out = []
+    for _ in range(2):
+        A = NUFFT(0)
+        A.plan(om, Nd, Kd, (J,) * len(Nd), batch=B, deterministic=True)
+        out.append((A.adjoint(y), A.y2k(y), A.solve(y, 'cg', maxiter=10)))
+        A.check()
+        A.release()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)

@@ -13,6 +13,8 @@
   deterministic gridding mode: forward rows against the FP64 NUDFT and the
   reference path planned on those rows, adjoint pixels against the NUDFT,
   two adjoints bitwise equal, and the adjoint identity over all samples.
+* solve(y, 'cg', maxiter=10) on the 8 coils of the kooshball's small case
+  (1M points, 96^3 / 192^3, deterministic), which the oracle can plan whole.
 * solve(y, 'cg', maxiter=20) on the 2D radial plan against the reference's
   own result (tests/golden/cg_c1.npz).
 
@@ -196,6 +198,35 @@ def test_kooshball_8_coils_deterministic_full_size(NUFFT):
         report('kooshball8.' + n, e)
     A.check()
     assert max(errs.values()) < TOL, errs
+
+
+def test_kooshball_8_coils_cg_10_small_case(NUFFT):
+    """solve(y, 'cg', maxiter=10) on every coil of an 8-coil kooshball plan in
+    the deterministic mode, on the small case of the 8M-point kooshball
+    (3,906 spokes x 256 samples, Nd 96^3, Kd 192^3: the same points per grid
+    cell, and a CSR the oracle can hold): coils 0 and 7 against the oracle's
+    CG on that coil within the float32-operator bound, and 3 iterations
+    within 1e-5."""
+    from pynufft_gb300.trajectories import kooshball_3d
+    om = kooshball_3d(3906, 256)
+    Nd, Kd, Jd, B = (96, 96, 96), (192, 192, 192), (6, 6, 6), 8
+    A = NUFFT(0)
+    A.plan(om, Nd, Kd, Jd, batch=B, deterministic=True)
+    y = cplx(np.random.default_rng(65), (om.shape[0], B))
+    x, it = A.solve(y, 'cg', maxiter=10, return_info=True)
+    x3 = A.solve(y, 'cg', maxiter=3)
+    assert it == 10
+    A.check()
+    O = OracleNUFFT()
+    O.plan(om, Nd, Kd, Jd, threads=THREADS)
+    for b in (0, B - 1):
+        xo = O.solve(y[:, b], 'cg', maxiter=10)
+        e = rel_l2(x[..., b], xo)
+        report(f'kooshball8_small.cg10_coil{b}', e)
+        assert e < cg_bound(O, y[:, b], 10, xo, f'kooshball8_small.cg10_coil{b}'), (b, e)
+        e3 = rel_l2(x3[..., b], O.solve(y[:, b], 'cg', maxiter=3))
+        report(f'kooshball8_small.cg3_coil{b}', e3)
+        assert e3 < TOL, (b, e3)
 
 
 def test_cg_radial_20_iterations_matches_reference(NUFFT):
