@@ -26,6 +26,9 @@
 
 namespace nufft {
 
+// Coils per lane group of the row kernels: 32 when they divide B, else 8.
+inline int cm_row_coils(int B) { return (B % 32 == 0) ? 32 : 8; }
+
 // Row slots of a warp: RS0 x RS1 (axis 0 x axis 1 rows) with RS0 * RS1 =
 // 32 / CB; 2D rows run along axis 1 and are indexed by axis 0 only.
 template <int DIM, int CB>
@@ -124,9 +127,11 @@ __device__ void sort_rows(int P, int nkey, KeyFn key, int* __restrict__ wcnt,
 // points and a block of nwarps warps: the staged per-point data
 // (coefficients, packed tile offsets, sample index) and the row sort's
 // histogram, offsets and list.
-__host__ __device__ inline size_t rows_smem(int DIM, int JM, int nkey, int P, int nwarps) {
-    return sizeof(float2) * (size_t)P * DIM * JM +
-           sizeof(int) * ((size_t)2 * P + (size_t)nwarps * nkey + nkey + 1 + P) + 16;
+__host__ __device__ inline size_t rows_smem(int DIM, int JM, int nkey, int P, int nwarps, int CB,
+                                            bool DET) {
+    const size_t ints = sizeof(int) * ((size_t)2 * P + (size_t)nwarps * nkey + nkey + 1 + P);
+    const size_t sy = (DIM == 2 && !DET) ? sizeof(float2) * (size_t)P * CB + 16 : 0;
+    return sizeof(float2) * (size_t)P * DIM * JM + ints + 16 + sy;
 }
 
 // Row gridding.  One block per row sub-problem: up to g.rgroup consecutive
@@ -150,12 +155,17 @@ __global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __r
     const int bs0 = g.bs[0], bs1 = (DIM == 3) ? g.bs[1] : 1;
     const int nkey = bs0 * bs1;
     const int nwarps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float2* scoef = reinterpret_cast<float2*>(smem_raw);                 // kRowSub x DIM x JM
-    int* sinfo = reinterpret_cast<int*>(scoef + (size_t)kRowSub * PC);   // pz | lx << 8 | ly << 16
-    int* sm = sinfo + kRowSub;                                           // sample index
-    int* wcnt = sm + kRowSub;
+    constexpr bool STAGEY = (DIM == 2 && !DET);   // samples staged in shared memory
+    constexpr int PCAP = (DIM == 2) ? kRowSub2 : kRowSub;   // points per sub-problem at most
+    float2* scoef = reinterpret_cast<float2*>(smem_raw);                 // PCAP x DIM x JM
+    int* sinfo = reinterpret_cast<int*>(scoef + (size_t)PCAP * PC);      // pz | lx << 8 | ly << 16
+    int* sm = sinfo + PCAP;                                              // sample index
+    int* wcnt = sm + PCAP;
     int* off = wcnt + nwarps * nkey;
     int* list = off + nkey + 1;
+    // STAGEY: the samples of the current coil chunk, PCAP x CB, 16-byte aligned
+    float2* sy = reinterpret_cast<float2*>(
+        (reinterpret_cast<uintptr_t>(list + PCAP) + 15) & ~static_cast<uintptr_t>(15));
 
     const int* __restrict__ pos0 = g.pos[0];
     const int* __restrict__ pos1 = g.pos[DIM == 3 ? 1 : 0];
@@ -216,6 +226,14 @@ __global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __r
     };
     for (int b0 = 0; b0 < B; b0 += CB) {
         const float2* __restrict__ yc = y + b0 + b;
+        if constexpr (STAGEY) {   // this chunk's samples, coalesced over the coils
+            __syncthreads();        // the previous chunk's samples are read
+            for (int e = threadIdx.x; e < P * CB; e += blockDim.x) {
+                const int j = e / CB, c = e - j * CB;
+                sy[e] = __ldg(y + (size_t)sm[j] * B + b0 + c);
+            }
+            __syncthreads();
+        }
         if (DIM == 3) {
             __syncthreads();   // every warp is done with the previous coil chunk
             if (threadIdx.x == 0) s_next_rb = nwarps;
@@ -235,10 +253,15 @@ __global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __r
                 if (j0 >= j1) continue;
                 touched = true;
                 const int ix = R0 + gx - lx;
-                float2 ynext = __ldg(yc + (size_t)sm[j0] * B);
+                float2 ynext = STAGEY ? make_float2(0.f, 0.f) : __ldg(yc + (size_t)sm[j0] * B);
                 for (int j = j0; j < j1; ++j) {
-                    const float2 yv = ynext;
-                    if (j + 1 < j1) ynext = __ldg(yc + (size_t)sm[j + 1] * B);
+                    float2 yv;
+                    if constexpr (STAGEY) {
+                        yv = sy[j * CB + b];
+                    } else {
+                        yv = ynext;
+                        if (j + 1 < j1) ynext = __ldg(yc + (size_t)sm[j + 1] * B);
+                    }
                     const int info = sinfo[j];
                     const float2* cj = scoef + (size_t)j * PC;
                     float2 w = make_float2(0.f, 0.f);

@@ -13,8 +13,6 @@ namespace nufft {
 template <int DIM>
 constexpr int cm_bin_z() { return 16; }
 
-// Coils per lane group of the row kernels: 32 when they divide B, else 8.
-inline int cm_row_coils(int B) { return (B % 32 == 0) ? 32 : 8; }
 
 template <int DIM, int JM, int CB, bool DET>
 static int y2k_rows_launch(const Geom& g, const float2* y, float2* grid, unsigned long long* igrid,
@@ -23,7 +21,7 @@ static int y2k_rows_launch(const Geom& g, const float2* y, float2* grid, unsigne
     auto kern = y2k_rows_kernel<DIM, JM, TZ, CB, DET>;
     const int threads = 256;
     const int nkey = g.bs[0] * (DIM == 3 ? g.bs[1] : 1);
-    const size_t smem = rows_smem(DIM, JM, nkey, kRowSub, threads / 32);
+    const size_t smem = rows_smem(DIM, JM, nkey, row_sub_cap(DIM), threads / 32, CB, DET);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);

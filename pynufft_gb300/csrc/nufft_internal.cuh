@@ -32,6 +32,13 @@ constexpr int kGatherSub = 512;
 // kRowSub points, so the tile's halo along that axis is shared.
 constexpr int kRowGroup = 4;
 constexpr int kRowSub = 512;
+// 2D row sub-problems hold at most kRowSub2 points: the fast row kernel
+// stages their samples (all coils of a lane group) in shared memory as well
+// (32-coil radial adjoint 0.447 -> 0.424 ms; the deterministic kernel, whose
+// extra sub-problems' 64-bit flushes cost more, 0.94 -> 0.975 ms, keeps the
+// same lists so that both modes' plans hold the same tables)
+constexpr int kRowSub2 = 256;
+inline int row_sub_cap(int ndim) { return ndim == 2 ? kRowSub2 : kRowSub; }
 
 void set_error(const std::string& msg);
 

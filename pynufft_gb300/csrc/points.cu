@@ -755,7 +755,7 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
         TRY_TMP(cudaGetLastError());
         TRY_TMP(cudaMalloc(&d_rnl, sizeof(int) * nlines));
         TRY_TMP(cudaMalloc(&d_rst, sizeof(int) * (nlines + 1)));
-        rowsub_kernel<<<lblocks, threads, 0, s>>>(d_start, nlines, nbz, p->rgroup, kRowSub,
+        rowsub_kernel<<<lblocks, threads, 0, s>>>(d_start, nlines, nbz, p->rgroup, row_sub_cap(nd),
                                                   nbin_inst, nullptr, d_rnl, nullptr);
         TRY_TMP(cudaGetLastError());
         scan_kernel<<<1, 1024, 0, s>>>(d_rnl, d_rst, nlines);
@@ -798,7 +798,7 @@ int set_points(nufft_plan_s* p, const int64_t* counts, const double* om, int om_
         p->nrsub = h_rnsub;
         TRY_TMP(cudaMalloc(&p->d_rsub, sizeof(int4) * std::max(h_rnsub, 1)));
         if (h_rnsub > 0) {
-            rowsub_kernel<<<lblocks, threads, 0, s>>>(d_start, nlines, nbz, p->rgroup, kRowSub,
+            rowsub_kernel<<<lblocks, threads, 0, s>>>(d_start, nlines, nbz, p->rgroup, row_sub_cap(nd),
                                                       nbin_inst, d_rst, nullptr, p->d_rsub);
             TRY_TMP(cudaGetLastError());
         }
