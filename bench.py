@@ -423,6 +423,9 @@ def main():
                     help='print only the multi-coil leg (a development aid; not a bench line)')
     ap.add_argument('--deterministic', action='store_true',
                     help='plan the workload in the deterministic gridding mode')
+    ap.add_argument('--fft', default='cufft', choices=['cufft', 'own'],
+                    help="the plan's image <-> spectrum transform (own: the library's pruned "
+                         'passes, one-coil power-of-two plans)')
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 5 if args.impl == 'reference' else 200
@@ -458,7 +461,7 @@ def main():
                         deterministic=args.deterministic)
         else:
             A.plan(om, c['Nd'], c['Kd'], c['Jd'], batch=c['batch'],
-                   deterministic=args.deterministic)
+                   deterministic=args.deterministic, fft=args.fft)
     make_plan()
     torch.cuda.synchronize()
     t0 = time.perf_counter()       # second plan: host om, tables rebuilt, no first-use costs
@@ -648,7 +651,8 @@ def main():
             'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
             'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'c64', 'data': 'synthetic',
-            'config': bench_config(args.config, world),
+            'config': dict(bench_config(args.config, world),
+                           **({'fft': args.fft} if args.fft != 'cufft' else {})),
             'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': ach, 'peak': peak,
                          'unit': 'GB/s', 'frac': ach / peak, 'peak_kind': peak_kind,
                          'traffic': traffic, 'alg_bytes': nbytes, 'ms': t_dom,

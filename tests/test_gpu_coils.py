@@ -102,3 +102,43 @@ def test_deterministic_plans_of_the_same_points_agree_bitwise(Nd, Kd, J, B):
         A.release()
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize('det', [False, True])
+def test_empty_and_ragged_coil_plans(det):
+    """Edge cases of the coil paths: a 3D 8-coil and a 2D 32-coil plan with
+    no points (forward gives (0, B), adjoint and y2k zeros, CG zeros); a
+    single point; and a many-instance coil plan whose middle instance has
+    no points while its neighbours match the oracle."""
+    from pynufft_gb300 import NUFFT
+    rng = np.random.default_rng(83)
+    for Nd, Kd, B in (((12, 14, 10), (24, 28, 20), 8), ((24, 20), (48, 40), 32)):
+        Jd = (6,) * len(Nd)
+        A = NUFFT(0)
+        A.plan(np.zeros((0, len(Nd))), Nd, Kd, Jd, batch=B, deterministic=det)
+        assert A.forward(cplx(rng, Nd + (B,))).shape == (0, B)
+        y0 = np.zeros((0, B), np.complex64)
+        assert not np.any(A.adjoint(y0)) and not np.any(A.y2k(y0))
+        assert not np.any(A.solve(y0, 'cg', maxiter=3))
+        A.check()
+        om = rng.uniform(-np.pi, np.pi, (1, len(Nd)))
+        A.plan(om, Nd, Kd, Jd, batch=B, deterministic=det)
+        O = OracleNUFFT()
+        O.plan(om, Nd, Kd, Jd, batch=B)
+        x, y = cplx(rng, Nd + (B,)), cplx(rng, (1, B))
+        assert rel_l2(A.forward(x), O.forward(x)) < TOL
+        assert rel_l2(A.adjoint(y), O.adjoint(y)) < TOL
+    Nd, Kd, Jd, B = (12, 14, 10), (24, 28, 20), (6, 6, 6), 8
+    oms = [rng.uniform(-np.pi, np.pi, (700, 3)), np.zeros((0, 3)), _points(rng, 900, 3)]
+    A = NUFFT(0)
+    A.plan_many(oms, Nd, Kd, Jd, batch=B, deterministic=det)
+    x = cplx(rng, (3,) + Nd + (B,))
+    y = cplx(rng, (1600, B))
+    yf, xa = A.forward(x), A.adjoint(y)
+    assert yf.shape == (1600, B) and not np.any(xa[1])
+    for i, (a, b) in ((0, (0, 700)), (2, (700, 1600))):
+        O = OracleNUFFT()
+        O.plan(oms[i], Nd, Kd, Jd, batch=B)
+        assert rel_l2(yf[a:b], O.forward(x[i])) < TOL
+        assert rel_l2(xa[i], O.adjoint(y[a:b])) < TOL
+    A.check()
