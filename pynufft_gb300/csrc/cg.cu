@@ -10,6 +10,8 @@
 // Every coil of every instance is an independent system with its own scalars.
 // All scalars live on the device: the loop of maxiter iterations is captured
 // once into a CUDA graph and replayed, with no host round trip per iteration.
+// p^H A p is evaluated as ||sp p||^2 from the interpolated samples, which
+// A = spH sp makes equal (the same quadratic form, one rounding apart).
 // A system that has met its tolerance freezes (its kernels skip it), which
 // reproduces the early return of scipy.  Vectors are complex64; the products
 // inside dots and norms are float32 and are accumulated in FP64 (runs of 8
@@ -147,9 +149,40 @@ __global__ void cg_update_p_kernel(CGGeom g, const CGSys* __restrict__ sys,
     }
 }
 
-__global__ void cg_dot_kernel(CGGeom g, const float2* __restrict__ p, const float2* __restrict__ q,
-                              double2* __restrict__ part) {
-    block_dot<false>(g, p, q, part);
+// p^H q with q = A^H A p is ||A p||^2: per-system partial sums of |y|^2 over
+// the system's samples y = A p (instance inst's points, coil b), which are
+// M-sized instead of prod(Kd)-sized (2M points: 16 MB read against the
+// 268 MB of p and q; same layout of partials as block_dot).
+__global__ void cg_ynorm_kernel(CGGeom g, const float2* __restrict__ yv,
+                                const int64_t* __restrict__ inst_start,
+                                double2* __restrict__ part) {
+    __shared__ double2 red[256];
+    const int inst = blockIdx.y;
+    const int t = threadIdx.x, b = t % g.B, q = t / g.B;
+    const int64_t m0 = inst_start[inst], mi = inst_start[inst + 1] - m0;
+    const int64_t chunk = (mi + g.nblk - 1) / g.nblk;
+    const int64_t c0 = blockIdx.x * chunk, c1 = min(mi, c0 + chunk);
+    double acc = 0.0;
+    int64_t c = c0 + q;
+    while (c < c1) {
+        float f = 0.f;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (c < c1) {
+                const float2 v = yv[(size_t)(m0 + c) * g.B + b];
+                f = fmaf(v.x, v.x, fmaf(v.y, v.y, f));
+            }
+            c += g.Q;
+        }
+        acc += f;
+    }
+    red[t] = make_double2(acc, 0.0);
+    __syncthreads();
+    for (int o = g.Q / 2; o > 0; o >>= 1) {
+        if (q < o) red[t].x += red[t + o * g.B].x;
+        __syncthreads();
+    }
+    if (q == 0) part[((size_t)inst * g.nblk + blockIdx.x) * g.B + b] = red[t];
 }
 
 __global__ void cg_alpha_kernel(CGGeom g, const double2* __restrict__ part, CGSys* __restrict__ sys) {
@@ -294,9 +327,9 @@ static int issue_iters(nufft_plan_s* p, const CGGeom& g, int iters, cudaStream_t
         cg_update_p_kernel<<<rgrid, rthreads, 0, s>>>(g, sys, r, pv);
         NUFFT_TRY(check_launch("cg_update_p_kernel"));
         NUFFT_TRY(launch_k2y(p, pv, p->d_ybuf, s));          // q = spH sp p
+        cg_ynorm_kernel<<<rgrid, rthreads, 0, s>>>(g, p->d_ybuf, p->d_inst_start, part);
+        NUFFT_TRY(check_launch("cg_ynorm_kernel"));           // p^H q = ||sp p||^2
         NUFFT_TRY(launch_y2k_grid(p, p->d_ybuf, q, s));
-        cg_dot_kernel<<<rgrid, rthreads, 0, s>>>(g, pv, q, part);
-        NUFFT_TRY(check_launch("cg_dot_kernel"));
         cg_alpha_kernel<<<g.S, kSumThreads, 0, s>>>(g, part, sys);
         NUFFT_TRY(check_launch("cg_alpha_kernel"));
         cg_axpy_kernel<<<rgrid, rthreads, 0, s>>>(g, sys, pv, q, xk, r, part);
