@@ -130,12 +130,12 @@ __device__ void sort_rows(int P, int nkey, KeyFn key, int* __restrict__ wcnt,
 __host__ __device__ inline size_t rows_smem(int DIM, int JM, int nkey, int P, int nwarps, int CB,
                                             bool DET) {
     const size_t ints = sizeof(int) * ((size_t)2 * P + (size_t)nwarps * nkey + nkey + 1 + P);
-    const size_t sy = (DIM == 2 && !DET) ? sizeof(float2) * (size_t)P * CB + 16 : 0;
+    const size_t sy = (DIM == 3 || !DET) ? sizeof(float2) * (size_t)P * CB + 16 : 0;
     return sizeof(float2) * (size_t)P * DIM * JM + ints + 16 + sy;
 }
 
 // Row gridding.  One block per row sub-problem: up to g.rgroup consecutive
-// bins along the innermost axis (3D), at most kRowSub points; the tile is
+// bins along the innermost axis (3D), at most row_sub_cap points; the tile is
 // (bs0 + J - 1) x (bs1 + J - 1) rows of TZ = rgroup * bs_z + J - 1 cells.
 template <int DIM, int JM, int TZ, int CB, bool DET>
 __global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __restrict__ y,
@@ -155,8 +155,8 @@ __global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __r
     const int bs0 = g.bs[0], bs1 = (DIM == 3) ? g.bs[1] : 1;
     const int nkey = bs0 * bs1;
     const int nwarps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr bool STAGEY = (DIM == 2 && !DET);   // samples staged in shared memory
-    constexpr int PCAP = (DIM == 2) ? kRowSub2 : kRowSub;   // points per sub-problem at most
+    constexpr bool STAGEY = (DIM == 3 || !DET);   // samples staged in shared memory
+    constexpr int PCAP = (DIM == 2) ? kRowSub2 : kRowSub3;   // points per sub-problem at most
     float2* scoef = reinterpret_cast<float2*>(smem_raw);                 // PCAP x DIM x JM
     int* sinfo = reinterpret_cast<int*>(scoef + (size_t)PCAP * PC);      // pz | lx << 8 | ly << 16
     int* sm = sinfo + PCAP;                                              // sample index

@@ -29,16 +29,17 @@ constexpr int kGatherSub = 512;
 
 // Row gridding (plans of 8 or more coils): a sub-problem takes up to
 // kRowGroup consecutive bins along the innermost axis (3D) and at most
-// kRowSub points, so the tile's halo along that axis is shared.
+// row_sub_cap points, so the tile's halo along that axis is shared.
 constexpr int kRowGroup = 4;
-constexpr int kRowSub = 512;
-// 2D row sub-problems hold at most kRowSub2 points: the fast row kernel
-// stages their samples (all coils of a lane group) in shared memory as well
-// (32-coil radial adjoint 0.447 -> 0.424 ms; the deterministic kernel, whose
-// extra sub-problems' 64-bit flushes cost more, 0.94 -> 0.975 ms, keeps the
-// same lists so that both modes' plans hold the same tables)
+// Row sub-problems hold at most kRowSub2 (2D) / kRowSub3 (3D) points, so
+// that the row kernels can stage their samples (all coils of a lane group)
+// in shared memory as well, two blocks per SM: 32-coil radial adjoint 0.447
+// -> 0.424 ms; 8-coil kooshball 21.2 -> 20.2 ms deterministic, 16.4 -> 15.5
+// ms fast.  The 2D deterministic kernel does not stage (0.97 against 1.00
+// ms) but keeps the same lists, so both modes' plans hold the same tables.
 constexpr int kRowSub2 = 256;
-inline int row_sub_cap(int ndim) { return ndim == 2 ? kRowSub2 : kRowSub; }
+constexpr int kRowSub3 = 448;
+inline int row_sub_cap(int ndim) { return ndim == 2 ? kRowSub2 : kRowSub3; }
 
 void set_error(const std::string& msg);
 
@@ -86,7 +87,7 @@ struct Geom {
     int64_t ngsub;               //   only past kGatherSub points
     const int4* rsub;            // row-gridding sub-problems (plans of 8+ coils):
     int64_t nrsub;               //   runs of <= kRowGroup bins along the innermost
-    int rgroup;                  //   axis (rgroup bins), <= kRowSub points
+    int rgroup;                  //   axis (rgroup bins), <= row_sub_cap points
     int kmethod;                 // k2y lane mapping (NUFFT_K2Y_*), resolved
     int ymethod;                 // y2k lane mapping (NUFFT_Y2K_*), resolved
     int* kerr;                   // device flag: a bounded wait ran out (nufft_plan_check)
