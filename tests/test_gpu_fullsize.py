@@ -12,7 +12,8 @@
 * 3D kooshball, 8 coils, M = 8,000,000 (Nd 192^3, Kd 384^3, Jd 6^3) in the
   deterministic gridding mode: forward rows against the FP64 NUDFT and the
   reference path planned on those rows, adjoint pixels against the NUDFT,
-  two adjoints bitwise equal, and the adjoint identity over all samples.
+  two adjoints bitwise equal (on one plan and on a second plan of the same
+  points), and the adjoint identity over all samples.
 * solve(y, 'cg', maxiter=10) on the 8 coils of the kooshball's small case
   (1M points, 96^3 / 192^3, deterministic), which the oracle can plan whole.
 * solve(y, 'cg', maxiter=20) on the 2D radial plan against the reference's
@@ -186,8 +187,12 @@ def test_kooshball_8_coils_deterministic_full_size(NUFFT):
     del C
     yr = cplx(rng, (M, B))
     xa = A.adjoint(yr)
-    xa2 = A.adjoint(yr)
-    assert np.array_equal(xa, xa2)
+    assert np.array_equal(xa, A.adjoint(yr))
+    A2 = NUFFT(0)    # a second plan of the same points: the same bits
+    A2.plan(om, Nd, Kd, Jd, batch=B, deterministic=True)
+    assert np.array_equal(xa, A2.adjoint(yr))
+    A2.release()
+    del A2
     pix = rng.choice(int(np.prod(Nd)), 64, replace=False)
     ref = nudft_adjoint_pixels(yr, om, Nd, pix) / np.prod(Kd)
     errs['adjoint_vs_nudft'] = rel_l2(xa.reshape(-1, B)[pix], ref)
