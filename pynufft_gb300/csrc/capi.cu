@@ -54,6 +54,7 @@ nufft::Geom nufft_plan_s::geom() const {
     g.rsub = d_rsub;
     g.nrsub = nrsub;
     g.rgroup = rgroup;
+    g.cm_il = cm_il ? 1 : 0;
     // lane mappings: coil-teams for B >= 8; otherwise the plan's choice.  The
     // defaults (fastest in measurement on 2D radial and 3D uniform
     // trajectories; the autotuner may pick others): k2y gathers from a shared

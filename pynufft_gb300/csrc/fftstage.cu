@@ -17,6 +17,7 @@ namespace nufft {
 
 struct ImgGeom {
     int ndim, B;
+    int il;           // coil-major spectra row-interleaved (2D, one instance)
     int N[3], K[3];
     int64_t prodN, prodK;
     int64_t n_img;    // ninst * prodN * B
@@ -28,6 +29,7 @@ static ImgGeom img_geom(const nufft_plan_s* p) {
     ImgGeom g{};
     g.ndim = p->ndim;
     g.B = p->B;
+    g.il = p->cm_il ? 1 : 0;
     int off = 0;
     for (int d = 0; d < 3; ++d) {
         g.N[d] = p->Nd[d];
@@ -214,6 +216,15 @@ __global__ void crop_rows_kernel(ImgGeom g, const float2* __restrict__ grid, flo
   }
 }
 
+// Element (leading row klocal, last-axis index k) of coil b of instance
+// inst in the coil-major spectra: system-contiguous, or row-interleaved
+// ((klocal B + b) K + k, one instance).
+__device__ __forceinline__ size_t cm_at(const ImgGeom& g, int64_t inst, int b, int64_t klocal,
+                                        int KL, int k) {
+    return g.il ? ((size_t)klocal * g.B + b) * KL + k
+                : ((size_t)inst * g.B + b) * g.prodK + (size_t)klocal * KL + k;
+}
+
 // Several coils, coil-major spectra.  The grid of system (instance, coil)
 // = inst * B + b is one contiguous Kd block of `cm`.  Pad: one block per grid
 // row (inst, leading indices) writes that row for every coil (zero outside
@@ -257,7 +268,7 @@ __global__ void pad_cm_rows_kernel(ImgGeom g, const float2* __restrict__ xx, flo
                 v = make_float2(a * v.y, -a * v.x);
             }
         }
-        cm[((size_t)inst * B + b) * g.prodK + (size_t)klocal * KL + k] = v;
+        cm[cm_at(g, inst, b, klocal, KL, k)] = v;
     }
   }
 }
@@ -296,6 +307,33 @@ __global__ void pad_cm_corner_kernel(ImgGeom g, const float2* __restrict__ xx,
   }
 }
 
+// Several coils, 2D, row-interleaved: image row n0 of every coil into the
+// zero-kept padded input (row n0 B + b, first N1 columns; the others are
+// never written), x sn, x -i (n_a - N_a/2) for the trajectory derivative.
+__global__ void pad_il_kernel(ImgGeom g, const float2* __restrict__ xx, float2* __restrict__ pad,
+                              int apply_sn, int dom_axis) {
+  for (int n0 = blockIdx.x; n0 < g.N[0]; n0 += gridDim.x) {
+    const int NL = g.N[1], KL = g.K[1], B = g.B;
+    const float s_lead = apply_sn ? __ldg(g.sn[0] + n0) : 1.f;
+    const float a_lead = (float)n0 - 0.5f * (float)g.N[0];
+    const float2* src = xx + (size_t)n0 * NL * B;
+    for (int e = threadIdx.x; e < NL * B; e += blockDim.x) {
+        const int b = e / NL, k = e - b * NL;
+        float2 v = __ldg(src + (size_t)k * B + b);
+        if (apply_sn) {
+            const float sc = s_lead * __ldg(g.sn[1] + k);
+            v.x *= sc;
+            v.y *= sc;
+        }
+        if (dom_axis >= 0) {
+            const float a = (dom_axis == 1) ? (float)k - 0.5f * (float)NL : a_lead;
+            v = make_float2(a * v.y, -a * v.x);
+        }
+        pad[((size_t)n0 * B + b) * KL + k] = v;
+    }
+  }
+}
+
 // Crop from coil-major spectra: one block per image row writes that row of
 // every coil into the coil-fastest image (x 1/prod(Kd), x sn if apply_sn,
 // / sn if divide_sn).
@@ -316,7 +354,7 @@ __global__ void crop_cm_rows_kernel(ImgGeom g, const float2* __restrict__ cm, fl
     float2* dst = xx + (size_t)r * NL * B;
     for (int e = threadIdx.x; e < NL * B; e += blockDim.x) {
         const int b = e / NL, k = e - b * NL;
-        float2 v = __ldg(cm + ((size_t)inst * B + b) * g.prodK + (size_t)klocal * KL + k);
+        float2 v = __ldg(cm + cm_at(g, inst, b, klocal, KL, k));
         float sc = norm;
         const float snv = s_lead * __ldg(g.sn[last] + k);
         if (apply_sn) sc *= snv;
@@ -459,6 +497,15 @@ static int coil_transpose(const nufft_plan_s* p, const float2* in, float2* out, 
 static int fft_cm_exec(nufft_plan_s* p, int direction, cudaStream_t s) {
     const int dir = (direction < 0) ? CUFFT_FORWARD : CUFFT_INVERSE;
     cufftComplex* cm = reinterpret_cast<cufftComplex*>(p->d_cm);
+    if (p->cm_il && dir == CUFFT_INVERSE) {
+        // columns, then only the first Nd[0] rows of every coil (the crop
+        // reads nothing else)
+        NUFFT_CUFFT_TRY(cufftSetStream(p->fft_cols, s));
+        NUFFT_CUFFT_TRY(cufftSetStream(p->fft_rows, s));
+        NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_cols, cm, cm, dir));
+        NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_rows, cm, cm, dir));
+        return NUFFT_OK;
+    }
     if (p->fft_cm_pruned) {
         NUFFT_CUFFT_TRY(cufftSetStream(p->fft_slab, s));
         NUFFT_CUFFT_TRY(cufftSetStream(p->fft_x, s));
@@ -516,6 +563,22 @@ int cm_to_grid(const nufft_plan_s* p, float2* k, cudaStream_t s) {
 // apply_sn), then the forward FFTs in place.
 int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s, int dom_axis) {
     ImgGeom g = img_geom(p);
+    if (p->cm_il) {
+        // 2D, row-interleaved: the image corner into the zero-kept padded
+        // rows, their row FFTs into the zero-kept row buffer, its column FFTs
+        // into the coil-major spectra
+        pad_il_kernel<<<row_blocks(p, g.N[0]), row_threads(g.N[1] * g.B), 0, s>>>(
+            g, xx, p->d_il_pad, apply_sn ? 1 : 0, dom_axis);
+        NUFFT_TRY(check_launch("pad_il_kernel"));
+        NUFFT_CUFFT_TRY(cufftSetStream(p->fft_rows, s));
+        NUFFT_CUFFT_TRY(cufftSetStream(p->fft_cols, s));
+        cufftComplex* pad = reinterpret_cast<cufftComplex*>(p->d_il_pad);
+        cufftComplex* z = reinterpret_cast<cufftComplex*>(p->d_il_z);
+        NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_rows, pad, z, CUFFT_FORWARD));
+        NUFFT_CUFFT_TRY(cufftExecC2C(p->fft_cols, z, reinterpret_cast<cufftComplex*>(p->d_cm),
+                                     CUFFT_FORWARD));
+        return NUFFT_OK;
+    }
     if (p->fft_cm_pruned && p->d_cmpad) {
         // 3D, a few systems: write only the Nd corners into the zero-kept
         // padded inputs; per system the (y, z) FFTs of its N0 slabs run out of
@@ -660,8 +723,9 @@ static int coil_transpose(const nufft_plan_s* p, const float2* in, float2* out, 
                           cudaStream_t s) {
     const int B = p->B;
     const int R = std::max(1, 1024 / B);
-    const int64_t cells = p->prodK;
-    const dim3 grid((unsigned)((cells + R - 1) / R), (unsigned)p->ninst);
+    // row-interleaved spectra: every grid row on its own (K1 cells x B coils)
+    const int64_t cells = p->cm_il ? p->Kd[1] : p->prodK;
+    const dim3 grid((unsigned)((cells + R - 1) / R), (unsigned)(p->cm_il ? p->Kd[0] : p->ninst));
     const size_t smem = sizeof(float2) * (size_t)B * (R + 1);
     if (to_major)
         to_coil_major_kernel<<<grid, 256, smem, s>>>(in, out, cells, B, R);
@@ -683,6 +747,18 @@ static int make_plan(cufftHandle* h, int rank, int* n, int stride, int dist, int
     size_t ws = 0;
     NUFFT_CUFFT_TRY(cufftMakePlanMany(*h, rank, n, n, stride, dist, n, stride, dist, CUFFT_C2C,
                                       batch, &ws));
+    *work = std::max(*work, ws);
+    return NUFFT_OK;
+}
+
+// A plan over embedded arrays: logical sizes n, storage inembed (= onembed).
+static int make_plan_embed(cufftHandle* h, int rank, int* n, int* embed, int stride, int dist,
+                           int batch, size_t* work) {
+    NUFFT_CUFFT_TRY(cufftCreate(h));
+    NUFFT_CUFFT_TRY(cufftSetAutoAllocation(*h, 0));
+    size_t ws = 0;
+    NUFFT_CUFFT_TRY(cufftMakePlanMany(*h, rank, n, embed, stride, dist, embed, stride, dist,
+                                      CUFFT_C2C, batch, &ws));
     *work = std::max(*work, ws);
     return NUFFT_OK;
 }
@@ -720,8 +796,19 @@ int fft_init(nufft_plan_s* p) {
     size_t work = 0;
     // one contiguous batched plan over every coil-major grid (B > 1 transforms
     // go through a coil-major copy: cuFFT's coil-strided transforms ran at
-    // under 1 TB/s)
-    NUFFT_TRY(make_plan(&p->fft, p->ndim, n, 1, (int)p->prodK, p->ninst * B, &work));
+    // under 1 TB/s); 2D plans of several coils and one instance keep the
+    // copy row-interleaved (nufft_plan_s::cm_il)
+    p->cm_il = (B > 1 && p->ndim == 2 && p->ninst == 1);
+    if (p->cm_il) {
+        int embed[2] = {p->Kd[0], B * p->Kd[1]};
+        NUFFT_TRY(make_plan_embed(&p->fft, 2, n, embed, 1, p->Kd[1], B, &work));
+        int nr[1] = {p->Kd[1]};
+        NUFFT_TRY(make_plan(&p->fft_rows, 1, nr, 1, p->Kd[1], p->Nd[0] * B, &work));
+        int nc[1] = {p->Kd[0]};
+        NUFFT_TRY(make_plan_embed(&p->fft_cols, 1, nc, nc, B * p->Kd[1], 1, B * p->Kd[1], &work));
+    } else {
+        NUFFT_TRY(make_plan(&p->fft, p->ndim, n, 1, (int)p->prodK, p->ninst * B, &work));
+    }
     if (B > 1) {
         const size_t ncm = (size_t)p->ninst * B * p->prodK;
         if (B > 1024 || ncm > ((size_t)1 << 40)) {
@@ -749,6 +836,15 @@ int fft_init(nufft_plan_s* p) {
         NUFFT_CUDA_TRY(cudaMalloc(&p->d_fftwork, work));
         p->dev_bytes += work;
     }
+    if (p->cm_il) {
+        // zero-kept padded rows (Nd[0] B rows) and row-FFT output (K0 B rows)
+        const size_t npad = (size_t)p->Nd[0] * B * p->Kd[1], nz = (size_t)p->prodK * B;
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_il_pad, sizeof(float2) * npad));
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_il_z, sizeof(float2) * nz));
+        NUFFT_CUDA_TRY(cudaMemset(p->d_il_pad, 0, sizeof(float2) * npad));
+        NUFFT_CUDA_TRY(cudaMemset(p->d_il_z, 0, sizeof(float2) * nz));
+        p->dev_bytes += sizeof(float2) * (npad + nz);
+    }
     if (p->fft_cm_pruned) {
         // per system a padded input (first Nd[0] slabs), one shared slab-FFT
         // output; both zero once, only their Nd corner / first Nd[0] slabs
@@ -774,6 +870,10 @@ int fft_init(nufft_plan_s* p) {
         NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_slab, p->d_fftwork));
         NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_x, p->d_fftwork));
     }
+    if (p->cm_il) {
+        NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_rows, p->d_fftwork));
+        NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_cols, p->d_fftwork));
+    }
     // own pruned passes where the grid allows (they use d_padin / d_slabout
     // as their intermediate arrays)
     return pfft_init(p);
@@ -785,7 +885,14 @@ void fft_destroy(nufft_plan_s* p) {
         cufftDestroy(p->fft_slab);
         cufftDestroy(p->fft_x);
     }
-    p->fft_ok = p->fft_pruned = p->fft_cm_pruned = false;
+    if (p->cm_il) {
+        cufftDestroy(p->fft_rows);
+        cufftDestroy(p->fft_cols);
+    }
+    p->fft_ok = p->fft_pruned = p->fft_cm_pruned = p->cm_il = false;
+    cudaFree(p->d_il_pad);
+    cudaFree(p->d_il_z);
+    p->d_il_pad = p->d_il_z = nullptr;
     pfft_free(p);
     cudaFree(p->d_fftwork);
     p->d_fftwork = nullptr;

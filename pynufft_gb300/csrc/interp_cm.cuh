@@ -291,7 +291,10 @@ __global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __r
                 }
                 // a row holds TZ <= Kz cells, so it wraps at most once: cells
                 // [0, cw) from o_z on, cells [cw, TZ) from 0
-                const size_t rbase = (ibase + b0 + b) * (size_t)g.prodK + row * Kz;
+                // (2D row-interleaved spectra: row X of coil b at (X B + b) Kz)
+                const size_t rbase = (DIM == 2 && g.cm_il)
+                                         ? (row * B + b0 + b) * (size_t)Kz
+                                         : (ibase + b0 + b) * (size_t)g.prodK + row * Kz;
                 const int cw = interior ? TZ : Kz - o[DI];
                 const size_t e0 = rbase + o[DI];
 #pragma unroll

@@ -88,6 +88,7 @@ struct Geom {
     const int4* rsub;            // row-gridding sub-problems (plans of 8+ coils):
     int64_t nrsub;               //   runs of <= kRowGroup bins along the innermost
     int rgroup;                  //   axis (rgroup bins), <= row_sub_cap points
+    int cm_il;                   // coil-major spectra row-interleaved (see nufft_plan_s)
     int kmethod;                 // k2y lane mapping (NUFFT_K2Y_*), resolved
     int ymethod;                 // y2k lane mapping (NUFFT_Y2K_*), resolved
     int* kerr;                   // device flag: a bounded wait ran out (nufft_plan_check)
@@ -211,6 +212,19 @@ struct nufft_plan_s {
     // Nd[0] stay zero), so the forward writes only the image corner
     float2* d_cmpad = nullptr;
     float2* d_cmslab = nullptr;
+    // 2D plans of several coils and one instance: the coil-major spectra are
+    // row-interleaved, cell (row r, coil b, column c) at (r B + b) K1 + c, so
+    // the first Nd[0] rows of every coil are one contiguous run and the row
+    // FFTs skip the zero rows (forward) and the rows the crop drops
+    // (inverse); fft_rows transforms those Nd[0] B rows, fft_cols the
+    // columns (stride B K1).  The forward pads the image corner into d_il_pad
+    // (Nd[0] B rows, columns past Nd[1] kept zero) and row-transforms it into
+    // d_il_z (rows past Nd[0] kept zero), whose columns transform into d_cm.
+    bool cm_il = false;
+    cufftHandle fft_rows = 0;
+    cufftHandle fft_cols = 0;
+    float2* d_il_pad = nullptr;
+    float2* d_il_z = nullptr;
     size_t dev_bytes = 0;
 
     nufft::Geom geom() const;
