@@ -216,13 +216,24 @@ __global__ void crop_rows_kernel(ImgGeom g, const float2* __restrict__ grid, flo
   }
 }
 
-// Element (leading row klocal, last-axis index k) of coil b of instance
-// inst in the coil-major spectra: system-contiguous, or row-interleaved
-// ((klocal B + b) K + k, one instance).
-__device__ __forceinline__ size_t cm_at(const ImgGeom& g, int64_t inst, int b, int64_t klocal,
-                                        int KL, int k) {
-    return g.il ? ((size_t)klocal * g.B + b) * KL + k
-                : ((size_t)inst * g.B + b) * g.prodK + (size_t)klocal * KL + k;
+// Element (leading indices n0[, n1], last-axis index k) of coil b of
+// instance inst in the coil-major spectra: system-contiguous, or interleaved
+// along the first axis (one instance): slab n0 of coil b at (n0 B + b) times
+// the slab size.
+template <int DIM>
+__device__ __forceinline__ size_t cm_at(const ImgGeom& g, int64_t inst, int b, int n0, int n1,
+                                        int k) {
+    constexpr int last = DIM - 1;
+    const int KL = g.K[last];
+    if (DIM == 1) return ((size_t)inst * g.B + b) * g.prodK + k;
+    if (g.il) {
+        size_t slab = (size_t)n0 * g.B + b;
+        if (DIM == 3) slab = slab * g.K[1] + n1;
+        return slab * KL + k;
+    }
+    size_t row = (size_t)n0;
+    if (DIM == 3) row = row * g.K[1] + n1;
+    return ((size_t)inst * g.B + b) * g.prodK + row * KL + k;
 }
 
 // Several coils, coil-major spectra.  The grid of system (instance, coil)
@@ -242,12 +253,9 @@ __global__ void pad_cm_rows_kernel(ImgGeom g, const float2* __restrict__ xx, flo
     constexpr int last = DIM - 1;
     const int KL = g.K[last], NL = g.N[last];
     const int B = g.B;
-    int64_t klocal = 0, xrow = inst;
+    int64_t xrow = inst;
 #pragma unroll
-    for (int d = 0; d < last; ++d) {
-        klocal = klocal * g.K[d] + n[d];
-        xrow = xrow * g.N[d] + n[d];
-    }
+    for (int d = 0; d < last; ++d) xrow = xrow * g.N[d] + n[d];
     const float s_lead = (apply_sn && inside) ? lead_sn<DIM>(g.sn[0], g.sn[1], n[0], n[1]) : 1.f;
     float a_lead = 0.f;
     if (DIM >= 2 && dom_axis == 0) a_lead = (float)n[0] - 0.5f * (float)g.N[0];
@@ -268,7 +276,7 @@ __global__ void pad_cm_rows_kernel(ImgGeom g, const float2* __restrict__ xx, flo
                 v = make_float2(a * v.y, -a * v.x);
             }
         }
-        cm[cm_at(g, inst, b, klocal, KL, k)] = v;
+        cm[cm_at<DIM>(g, inst, b, n[0], n[1], k)] = v;
     }
   }
 }
@@ -307,29 +315,37 @@ __global__ void pad_cm_corner_kernel(ImgGeom g, const float2* __restrict__ xx,
   }
 }
 
-// Several coils, 2D, row-interleaved: image row n0 of every coil into the
-// zero-kept padded input (row n0 B + b, first N1 columns; the others are
-// never written), x sn, x -i (n_a - N_a/2) for the trajectory derivative.
+// Several coils, interleaved spectra: image row (n0[, n1]) of every coil
+// into the zero-kept padded input (slab n0 B + b, only the Nd corner; the
+// rest is never written), x sn, x -i (n_a - N_a/2) for the trajectory
+// derivative.
+template <int DIM>
 __global__ void pad_il_kernel(ImgGeom g, const float2* __restrict__ xx, float2* __restrict__ pad,
-                              int apply_sn, int dom_axis) {
-  for (int n0 = blockIdx.x; n0 < g.N[0]; n0 += gridDim.x) {
-    const int NL = g.N[1], KL = g.K[1], B = g.B;
-    const float s_lead = apply_sn ? __ldg(g.sn[0] + n0) : 1.f;
-    const float a_lead = (float)n0 - 0.5f * (float)g.N[0];
-    const float2* src = xx + (size_t)n0 * NL * B;
+                              int apply_sn, int dom_axis, int64_t rows) {
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    int64_t inst;
+    int n[3] = {0, 0, 0};
+    row_index<DIM>(r, g.N[0], g.N[1], inst, n[0], n[1]);
+    constexpr int last = DIM - 1;
+    const int NL = g.N[last], B = g.B;
+    const float s_lead = apply_sn ? lead_sn<DIM>(g.sn[0], g.sn[1], n[0], n[1]) : 1.f;
+    float a_lead = 0.f;
+    if (dom_axis == 0) a_lead = (float)n[0] - 0.5f * (float)g.N[0];
+    if (DIM == 3 && dom_axis == 1) a_lead = (float)n[1] - 0.5f * (float)g.N[1];
+    const float2* src = xx + (size_t)r * NL * B;
     for (int e = threadIdx.x; e < NL * B; e += blockDim.x) {
         const int b = e / NL, k = e - b * NL;
         float2 v = __ldg(src + (size_t)k * B + b);
         if (apply_sn) {
-            const float sc = s_lead * __ldg(g.sn[1] + k);
+            const float sc = s_lead * __ldg(g.sn[last] + k);
             v.x *= sc;
             v.y *= sc;
         }
         if (dom_axis >= 0) {
-            const float a = (dom_axis == 1) ? (float)k - 0.5f * (float)NL : a_lead;
+            const float a = (dom_axis == last) ? (float)k - 0.5f * (float)NL : a_lead;
             v = make_float2(a * v.y, -a * v.x);
         }
-        pad[((size_t)n0 * B + b) * KL + k] = v;
+        pad[cm_at<DIM>(g, 0, b, n[0], n[1], k)] = v;
     }
   }
 }
@@ -348,13 +364,10 @@ __global__ void crop_cm_rows_kernel(ImgGeom g, const float2* __restrict__ cm, fl
     const int KL = g.K[last], NL = g.N[last];
     const int B = g.B;
     const float s_lead = lead_sn<DIM>(g.sn[0], g.sn[1], n[0], n[1]);
-    int64_t klocal = 0;
-#pragma unroll
-    for (int d = 0; d < last; ++d) klocal = klocal * g.K[d] + n[d];
     float2* dst = xx + (size_t)r * NL * B;
     for (int e = threadIdx.x; e < NL * B; e += blockDim.x) {
         const int b = e / NL, k = e - b * NL;
-        float2 v = __ldg(cm + cm_at(g, inst, b, klocal, KL, k));
+        float2 v = __ldg(cm + cm_at<DIM>(g, inst, b, n[0], n[1], k));
         float sc = norm;
         const float snv = s_lead * __ldg(g.sn[last] + k);
         if (apply_sn) sc *= snv;
@@ -564,11 +577,19 @@ int cm_to_grid(const nufft_plan_s* p, float2* k, cudaStream_t s) {
 int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s, int dom_axis) {
     ImgGeom g = img_geom(p);
     if (p->cm_il) {
-        // 2D, row-interleaved: the image corner into the zero-kept padded
-        // rows, their row FFTs into the zero-kept row buffer, its column FFTs
-        // into the coil-major spectra
-        pad_il_kernel<<<row_blocks(p, g.N[0]), row_threads(g.N[1] * g.B), 0, s>>>(
-            g, xx, p->d_il_pad, apply_sn ? 1 : 0, dom_axis);
+        // interleaved: the image corner into the zero-kept padded slabs,
+        // their (inner-axes) FFTs into the zero-kept slab buffer, its
+        // first-axis FFTs into the coil-major spectra
+        // (the padded input holds the first Nd[0] slabs of every coil, laid
+        // out like the spectra's first Nd[0] B slabs)
+        const int64_t rows = rows_of(g, g.N, 1);
+        const unsigned nb = row_blocks(p, rows);
+        const int nt = row_threads(g.N[g.ndim - 1] * g.B);
+        const int as = apply_sn ? 1 : 0;
+        if (p->ndim == 2)
+            pad_il_kernel<2><<<nb, nt, 0, s>>>(g, xx, p->d_il_pad, as, dom_axis, rows);
+        else
+            pad_il_kernel<3><<<nb, nt, 0, s>>>(g, xx, p->d_il_pad, as, dom_axis, rows);
         NUFFT_TRY(check_launch("pad_il_kernel"));
         NUFFT_CUFFT_TRY(cufftSetStream(p->fft_rows, s));
         NUFFT_CUFFT_TRY(cufftSetStream(p->fft_cols, s));
@@ -723,8 +744,9 @@ static int coil_transpose(const nufft_plan_s* p, const float2* in, float2* out, 
                           cudaStream_t s) {
     const int B = p->B;
     const int R = std::max(1, 1024 / B);
-    // row-interleaved spectra: every grid row on its own (K1 cells x B coils)
-    const int64_t cells = p->cm_il ? p->Kd[1] : p->prodK;
+    // interleaved spectra: every first-axis slab on its own (prod(Kd) / K0
+    // cells x B coils)
+    const int64_t cells = p->cm_il ? p->prodK / p->Kd[0] : p->prodK;
     const dim3 grid((unsigned)((cells + R - 1) / R), (unsigned)(p->cm_il ? p->Kd[0] : p->ninst));
     const size_t smem = sizeof(float2) * (size_t)B * (R + 1);
     if (to_major)
@@ -798,14 +820,19 @@ int fft_init(nufft_plan_s* p) {
     // go through a coil-major copy: cuFFT's coil-strided transforms ran at
     // under 1 TB/s); 2D plans of several coils and one instance keep the
     // copy row-interleaved (nufft_plan_s::cm_il)
-    p->cm_il = (B > 1 && p->ndim == 2 && p->ninst == 1);
+    // (3D: only up to 1 GiB of spectra -- 8 coils at 192^3: pair 3.95 -> 3.74
+    // ms; at 384^3, 3.6 GB, the per-system pruned plans below were 1.5%
+    // faster: 31.1 against 31.5 ms)
+    p->cm_il = (B > 1 && p->ninst == 1 &&
+                (p->ndim == 2 ||
+                 (p->ndim == 3 && sizeof(float2) * (size_t)B * p->prodK <= ((size_t)1 << 30))));
     if (p->cm_il) {
-        int embed[2] = {p->Kd[0], B * p->Kd[1]};
-        NUFFT_TRY(make_plan_embed(&p->fft, 2, n, embed, 1, p->Kd[1], B, &work));
-        int nr[1] = {p->Kd[1]};
-        NUFFT_TRY(make_plan(&p->fft_rows, 1, nr, 1, p->Kd[1], p->Nd[0] * B, &work));
+        const int slab = (int)(p->prodK / p->Kd[0]);   // cells of a first-axis slab
+        int embed[3] = {p->Kd[0], B * p->Kd[1], p->ndim == 3 ? p->Kd[2] : 1};
+        NUFFT_TRY(make_plan_embed(&p->fft, p->ndim, n, embed, 1, slab, B, &work));
+        NUFFT_TRY(make_plan(&p->fft_rows, p->ndim - 1, n + 1, 1, slab, p->Nd[0] * B, &work));
         int nc[1] = {p->Kd[0]};
-        NUFFT_TRY(make_plan_embed(&p->fft_cols, 1, nc, nc, B * p->Kd[1], 1, B * p->Kd[1], &work));
+        NUFFT_TRY(make_plan_embed(&p->fft_cols, 1, nc, nc, B * slab, 1, B * slab, &work));
     } else {
         NUFFT_TRY(make_plan(&p->fft, p->ndim, n, 1, (int)p->prodK, p->ninst * B, &work));
     }
@@ -824,7 +851,7 @@ int fft_init(nufft_plan_s* p) {
         NUFFT_TRY(make_plan(&p->fft_slab, p->ndim - 1, n + 1, 1, slab, p->Nd[0], &work));
         NUFFT_TRY(make_plan(&p->fft_x, 1, n, slab, 1, slab, &work));
         p->fft_pruned = true;
-    } else if (B > 1 && p->ndim == 3 && p->Nd[0] < p->Kd[0] && p->ninst * B <= 16) {
+    } else if (B > 1 && !p->cm_il && p->ndim == 3 && p->Nd[0] < p->Kd[0] && p->ninst * B <= 16) {
         // coil-major spectra of a few 3D systems: the same pruned pair of
         // plans, run once per system
         const int slab = (int)(p->prodK / p->Kd[0]);
@@ -837,8 +864,9 @@ int fft_init(nufft_plan_s* p) {
         p->dev_bytes += work;
     }
     if (p->cm_il) {
-        // zero-kept padded rows (Nd[0] B rows) and row-FFT output (K0 B rows)
-        const size_t npad = (size_t)p->Nd[0] * B * p->Kd[1], nz = (size_t)p->prodK * B;
+        // zero-kept padded slabs (Nd[0] B of them) and slab-FFT output (K0 B)
+        const size_t npad = (size_t)p->Nd[0] * B * (p->prodK / p->Kd[0]);
+        const size_t nz = (size_t)p->prodK * B;
         NUFFT_CUDA_TRY(cudaMalloc(&p->d_il_pad, sizeof(float2) * npad));
         NUFFT_CUDA_TRY(cudaMalloc(&p->d_il_z, sizeof(float2) * nz));
         NUFFT_CUDA_TRY(cudaMemset(p->d_il_pad, 0, sizeof(float2) * npad));

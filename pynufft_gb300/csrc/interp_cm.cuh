@@ -281,20 +281,21 @@ __global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __r
             // flush each lane's row (row slot, coil) straight from registers
             const int rx = R0 + gx, ry = R1 + gy;
             if (rx < T0 && ry < T1) {
-                size_t row;
+                // the row's first cell: system-contiguous spectra, or
+                // interleaved along the first axis (slab X of coil b at
+                // (X B + b) times the slab size)
+                const size_t X = interior ? o[0] + rx : wrapn(o[0] + rx, g.K[0]);
+                size_t rbase;
                 if constexpr (DIM == 3) {
-                    const int X = interior ? o[0] + rx : wrapn(o[0] + rx, g.K[0]);
-                    const int Y = interior ? o[1] + ry : wrapn(o[1] + ry, g.K[1]);
-                    row = (size_t)X * g.K[1] + Y;
+                    const size_t Y = interior ? o[1] + ry : wrapn(o[1] + ry, g.K[1]);
+                    rbase = g.cm_il ? ((X * B + b0 + b) * g.K[1] + Y) * Kz
+                                    : (ibase + b0 + b) * (size_t)g.prodK + (X * g.K[1] + Y) * Kz;
                 } else {
-                    row = (size_t)(interior ? o[0] + rx : wrapn(o[0] + rx, g.K[0]));
+                    rbase = g.cm_il ? (X * B + b0 + b) * Kz
+                                    : (ibase + b0 + b) * (size_t)g.prodK + X * Kz;
                 }
                 // a row holds TZ <= Kz cells, so it wraps at most once: cells
                 // [0, cw) from o_z on, cells [cw, TZ) from 0
-                // (2D row-interleaved spectra: row X of coil b at (X B + b) Kz)
-                const size_t rbase = (DIM == 2 && g.cm_il)
-                                         ? (row * B + b0 + b) * (size_t)Kz
-                                         : (ibase + b0 + b) * (size_t)g.prodK + row * Kz;
                 const int cw = interior ? TZ : Kz - o[DI];
                 const size_t e0 = rbase + o[DI];
 #pragma unroll

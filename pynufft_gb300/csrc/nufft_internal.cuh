@@ -212,14 +212,16 @@ struct nufft_plan_s {
     // Nd[0] stay zero), so the forward writes only the image corner
     float2* d_cmpad = nullptr;
     float2* d_cmslab = nullptr;
-    // 2D plans of several coils and one instance: the coil-major spectra are
-    // row-interleaved, cell (row r, coil b, column c) at (r B + b) K1 + c, so
-    // the first Nd[0] rows of every coil are one contiguous run and the row
-    // FFTs skip the zero rows (forward) and the rows the crop drops
-    // (inverse); fft_rows transforms those Nd[0] B rows, fft_cols the
-    // columns (stride B K1).  The forward pads the image corner into d_il_pad
-    // (Nd[0] B rows, columns past Nd[1] kept zero) and row-transforms it into
-    // d_il_z (rows past Nd[0] kept zero), whose columns transform into d_cm.
+    // Plans of several coils and one instance (2D, 3D): the coil-major
+    // spectra are interleaved along the first axis, first-axis slab n0 of
+    // coil b at (n0 B + b) times the slab size (prod(Kd) / K0), so the first
+    // Nd[0] slabs of every coil are one contiguous run and the inner-axes
+    // FFTs (fft_rows) skip the zero slabs (forward) and the slabs the crop
+    // drops (inverse); fft_cols transforms along the first axis (stride B
+    // times the slab size).  The forward pads the image corner into d_il_pad
+    // (Nd[0] B slabs, kept zero outside the corner), transforms its slabs
+    // into d_il_z (slabs past Nd[0] kept zero), whose first axis transforms
+    // into d_cm.
     bool cm_il = false;
     cufftHandle fft_rows = 0;
     cufftHandle fft_cols = 0;
