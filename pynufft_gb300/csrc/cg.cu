@@ -27,6 +27,7 @@ struct CGSys {
     double rho, rho_prev, tol;
     double pq_re, pq_im, al_re, al_im;
     int done, iters, breakdown, maxiter;
+    int xpend;   // x += alpha p of the last step not applied yet
 };
 
 struct CGGeom {
@@ -125,27 +126,64 @@ __global__ void cg_init_sys_kernel(CGGeom g, const double2* __restrict__ part,
     sys[s] = st;
 }
 
-// p = r (first iteration) or p = r + beta p; grid (nblk, ninst), thread t
-// serves coil t % B like the reductions
+// x += alpha p for the previous step (deferred from cg_axpy_kernel, so that
+// pass reads neither x nor p: the same operations on the same values, one
+// pass later), then p = r (first iteration) or p = r + beta p; grid (nblk,
+// ninst), thread t serves coil t % B like the reductions
 __global__ void cg_update_p_kernel(CGGeom g, const CGSys* __restrict__ sys,
-                                   const float2* __restrict__ r, float2* __restrict__ p) {
+                                   const float2* __restrict__ r, float2* __restrict__ p,
+                                   float2* __restrict__ x) {
     const int inst = blockIdx.y;
     const int t = threadIdx.x, b = t % g.B, q = t / g.B;
     const CGSys& st = sys[inst * g.B + b];
-    if (st.done) return;
-    const bool first = st.iters == 0;
+    const bool ux = st.xpend, up = !st.done;
+    if (!ux && !up) return;
+    const bool first = st.iters == 0;   // (nothing is pending then)
     const float beta = first ? 0.f : (float)(st.rho / st.rho_prev);
+    const float ar = (float)st.al_re, ai = (float)st.al_im;
     const int64_t chunk = (g.prodK + g.nblk - 1) / g.nblk;
     const int64_t c0 = blockIdx.x * chunk, c1 = min(g.prodK, c0 + chunk);
     for (int64_t c = c0 + q; c < c1; c += g.Q) {
         const size_t e = ((size_t)inst * g.prodK + c) * g.B + b;
-        const float2 rv = r[e];
-        if (first) {
-            p[e] = rv;
-        } else {
+        if (ux) {
             const float2 pv = p[e];
-            p[e] = make_float2(fmaf(beta, pv.x, rv.x), fmaf(beta, pv.y, rv.y));
+            float2 xv = x[e];
+            xv.x = fmaf(ar, pv.x, fmaf(-ai, pv.y, xv.x));
+            xv.y = fmaf(ar, pv.y, fmaf(ai, pv.x, xv.y));
+            x[e] = xv;
+            if (up) {
+                const float2 rv = r[e];
+                p[e] = make_float2(fmaf(beta, pv.x, rv.x), fmaf(beta, pv.y, rv.y));
+            }
+        } else {
+            const float2 rv = r[e];
+            if (first) {
+                p[e] = rv;
+            } else {
+                const float2 pv = p[e];
+                p[e] = make_float2(fmaf(beta, pv.x, rv.x), fmaf(beta, pv.y, rv.y));
+            }
         }
+    }
+}
+
+// the step still pending after the last iteration: x += alpha p
+__global__ void cg_xflush_kernel(CGGeom g, const CGSys* __restrict__ sys,
+                                 const float2* __restrict__ p, float2* __restrict__ x) {
+    const int inst = blockIdx.y;
+    const int t = threadIdx.x, b = t % g.B, q = t / g.B;
+    const CGSys& st = sys[inst * g.B + b];
+    if (!st.xpend) return;
+    const float ar = (float)st.al_re, ai = (float)st.al_im;
+    const int64_t chunk = (g.prodK + g.nblk - 1) / g.nblk;
+    const int64_t c0 = blockIdx.x * chunk, c1 = min(g.prodK, c0 + chunk);
+    for (int64_t c = c0 + q; c < c1; c += g.Q) {
+        const size_t e = ((size_t)inst * g.prodK + c) * g.B + b;
+        const float2 pv = p[e];
+        float2 xv = x[e];
+        xv.x = fmaf(ar, pv.x, fmaf(-ai, pv.y, xv.x));
+        xv.y = fmaf(ar, pv.y, fmaf(ai, pv.x, xv.y));
+        x[e] = xv;
     }
 }
 
@@ -187,7 +225,11 @@ __global__ void cg_ynorm_kernel(CGGeom g, const float2* __restrict__ yv,
 
 __global__ void cg_alpha_kernel(CGGeom g, const double2* __restrict__ part, CGSys* __restrict__ sys) {
     const int s = blockIdx.x;   // one block per system
-    if (sys[s].done) return;
+    if (sys[s].done) {
+        // this iteration's cg_update_p_kernel has applied its pending step
+        if (threadIdx.x == 0) sys[s].xpend = 0;
+        return;
+    }
     const double2 pq = sum_parts(g, part, s);
     if (threadIdx.x != 0) return;
     CGSys st = sys[s];
@@ -198,17 +240,19 @@ __global__ void cg_alpha_kernel(CGGeom g, const double2* __restrict__ part, CGSy
         st.breakdown = 1;
         st.done = 1;
         st.al_re = st.al_im = 0.0;
+        st.xpend = 0;
     } else {
-        // alpha = rho / pq (complex)
+        // alpha = rho / pq (complex); x += alpha p follows in the next update
         st.al_re = st.rho * pq.x / den;
         st.al_im = -st.rho * pq.y / den;
+        st.xpend = 1;
     }
     sys[s] = st;
 }
 
-// x += alpha p; r -= alpha q; partial ||r||^2
-__global__ void cg_axpy_kernel(CGGeom g, const CGSys* __restrict__ sys, const float2* __restrict__ p,
-                               const float2* __restrict__ q, float2* __restrict__ x,
+// r -= alpha q; partial ||r||^2 (x += alpha p waits for the next
+// cg_update_p_kernel, which reads p anyway)
+__global__ void cg_axpy_kernel(CGGeom g, const CGSys* __restrict__ sys, const float2* __restrict__ q,
                                float2* __restrict__ r, double2* __restrict__ part) {
     __shared__ double2 red[256];
     const int inst = blockIdx.y;
@@ -228,13 +272,9 @@ __global__ void cg_axpy_kernel(CGGeom g, const CGSys* __restrict__ sys, const fl
                 const size_t e = ((size_t)inst * g.prodK + c) * g.B + b;
                 float2 rv = r[e];
                 if (active) {
-                    const float2 pv = p[e], qv = q[e];
-                    float2 xv = x[e];
-                    xv.x = fmaf(ar, pv.x, fmaf(-ai, pv.y, xv.x));
-                    xv.y = fmaf(ar, pv.y, fmaf(ai, pv.x, xv.y));
+                    const float2 qv = q[e];
                     rv.x = fmaf(-ar, qv.x, fmaf(ai, qv.y, rv.x));
                     rv.y = fmaf(-ar, qv.y, fmaf(-ai, qv.x, rv.y));
-                    x[e] = xv;
                     r[e] = rv;
                 }
                 f = fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, f));
@@ -324,7 +364,7 @@ static int issue_iters(nufft_plan_s* p, const CGGeom& g, int iters, cudaStream_t
     const dim3 rgrid(g.nblk, g.ninst);
     const int rthreads = g.B * g.Q;
     for (int it = 0; it < iters; ++it) {
-        cg_update_p_kernel<<<rgrid, rthreads, 0, s>>>(g, sys, r, pv);
+        cg_update_p_kernel<<<rgrid, rthreads, 0, s>>>(g, sys, r, pv, xk);
         NUFFT_TRY(check_launch("cg_update_p_kernel"));
         NUFFT_TRY(launch_k2y(p, pv, p->d_ybuf, s));          // q = spH sp p
         cg_ynorm_kernel<<<rgrid, rthreads, 0, s>>>(g, p->d_ybuf, p->d_inst_start, part);
@@ -332,7 +372,7 @@ static int issue_iters(nufft_plan_s* p, const CGGeom& g, int iters, cudaStream_t
         NUFFT_TRY(launch_y2k_grid(p, p->d_ybuf, q, s));
         cg_alpha_kernel<<<g.S, kSumThreads, 0, s>>>(g, part, sys);
         NUFFT_TRY(check_launch("cg_alpha_kernel"));
-        cg_axpy_kernel<<<rgrid, rthreads, 0, s>>>(g, sys, pv, q, xk, r, part);
+        cg_axpy_kernel<<<rgrid, rthreads, 0, s>>>(g, sys, q, r, part);
         NUFFT_TRY(check_launch("cg_axpy_kernel"));
         cg_finalize_kernel<<<g.S, kSumThreads, 0, s>>>(g, part, sys);
         NUFFT_TRY(check_launch("cg_finalize_kernel"));
@@ -416,8 +456,14 @@ int solve_cg(nufft_plan_s* p, const float2* y, float2* x, int maxiter, double rt
         if (all) break;
     }
 
-    // k-space solution -> image: k2xx then divide by sn
+    // the last step, then the k-space solution -> image: k2xx, divide by sn
     float2* xk = p->d_cg;
+    {
+        const dim3 rgrid(g.nblk, g.ninst);
+        cg_xflush_kernel<<<rgrid, g.B * g.Q, 0, s>>>(g, reinterpret_cast<const CGSys*>(p->d_cgs),
+                                                     xk + 2 * n, xk);
+        NUFFT_TRY(check_launch("cg_xflush_kernel"));
+    }
     NUFFT_TRY(image_from_spectrum(p, xk, x, false, true, s));
 
     if (iters_out) {
