@@ -423,9 +423,9 @@ def main():
                     help='print only the multi-coil leg (a development aid; not a bench line)')
     ap.add_argument('--deterministic', action='store_true',
                     help='plan the workload in the deterministic gridding mode')
-    ap.add_argument('--fft', default='cufft', choices=['cufft', 'own'],
-                    help="the plan's image <-> spectrum transform (own: the library's pruned "
-                         'passes, one-coil power-of-two plans)')
+    ap.add_argument('--fft', default='auto', choices=['auto', 'cufft', 'own'],
+                    help="the plan's image <-> spectrum transform (auto: the library's choice; "
+                         "own: its pruned passes, one-coil power-of-two plans; cufft)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 5 if args.impl == 'reference' else 200
@@ -652,7 +652,7 @@ def main():
             'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'c64', 'data': 'synthetic',
             'config': dict(bench_config(args.config, world),
-                           **({'fft': args.fft} if args.fft != 'cufft' else {})),
+                           **({'fft': args.fft} if args.fft != 'auto' else {})),
             'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': ach, 'peak': peak,
                          'unit': 'GB/s', 'frac': ach / peak, 'peak_kind': peak_kind,
                          'traffic': traffic, 'alg_bytes': nbytes, 'ms': t_dom,

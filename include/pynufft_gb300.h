@@ -50,6 +50,8 @@ extern "C" {
                                        FFT passes instead of cuFFT, where the
                                        plan allows them (see
                                        nufft_plan_transform_kind)             */
+#define NUFFT_FLAG_CUFFT         4  /* cuFFT even where the own passes would
+                                       be chosen without a flag               */
 
 typedef struct nufft_plan_s* nufft_plan_t;
 
@@ -162,9 +164,11 @@ int nufft_plan_info(nufft_plan_t plan, int64_t* M_total, int64_t* n_subproblems,
 /* Which transform the image <-> spectrum stages of this plan run:
  * NUFFT_FFT_CUFFT (cuFFT over the whole padded grid), NUFFT_FFT_CUFFT_PRUNED
  * (cuFFT on the slabs the padding leaves nonzero), NUFFT_FFT_OWN_PRUNED (the
- * library's pruned power-of-two passes: NUFFT_FLAG_OWN_FFT set, one coil,
- * one instance, 2D/3D, Nd[0] < Kd[0], every Kd a power of two in 16..4096).
- * No counterpart in the reference (numpy fftn / ifftn). */
+ * library's pruned power-of-two passes: one coil, one instance, 2D/3D,
+ * Nd[0] < Kd[0], every Kd a power of two in 16..4096, and either
+ * NUFFT_FLAG_OWN_FFT set or -- without NUFFT_FLAG_CUFFT -- every Kd 256 and
+ * every Nd 128 or 256, where the passes' specialised 256-point kernels beat
+ * cuFFT).  No counterpart in the reference (numpy fftn / ifftn). */
 #define NUFFT_FFT_CUFFT        0
 #define NUFFT_FFT_CUFFT_PRUNED 1
 #define NUFFT_FFT_OWN_PRUNED   2

@@ -1,6 +1,7 @@
 // Pruned power-of-two FFTs of one coil and one instance (2D and 3D plans
 // whose every Kd is a power of two, 16 .. 4096), used when the plan asks for
-// them (NUFFT_FLAG_OWN_FFT); plans otherwise run cuFFT.
+// them (NUFFT_FLAG_OWN_FFT) and, unless it asks for cuFFT (NUFFT_FLAG_CUFFT),
+// by default where every pass is a 256-point one; plans otherwise run cuFFT.
 //
 // The reference's xx2k zero-pads the image into the Kd array and runs numpy's
 // fftn over it (_xx2k_cpu, nufft/_nufft_class_methods_cpu.py:232-249); k2xx
@@ -26,11 +27,14 @@
 // butterflies' strided writes fall in distinct banks.  Entries past the input
 // extent are zero in registers and never loaded; entries past the output
 // extent are never stored.  At Kd = 2 Nd this moves 352 MB per 256^3
-// transform instead of the ~570 MB of the zero-padded cuFFT passes, but on a
-// GB300 the passes run at ~3 TB/s: 0.125 / 0.128 ms forward / inverse at
-// 256^3 against cuFFT's 0.110 / ~0.105 ms (and 0.019 / 0.019 against 0.015 /
-// 0.020 ms at 512^2), so cuFFT stays the default.  T1 and T2 live in the
-// plan's d_padin / d_slabout buffers.
+// transform instead of the ~570 MB of the zero-padded cuFFT passes.  These
+// general passes are bound by instruction issue (~3 TB/s: 0.125 / 0.128 ms
+// forward / inverse at 256^3 against cuFFT's 0.110 / ~0.105 ms; 0.019 /
+// 0.019 against 0.015 / 0.020 ms at 512^2); 256-point passes run
+// pfft256_kernel instead, with every size fixed at compile time (0.077 /
+// 0.091 ms at 256^3 against 0.111 / 0.146 for the cuFFT stages with their
+// pad and crop), which is why those plans take the own passes by default.
+// T1 and T2 live in the plan's d_padin / d_slabout buffers.
 #include "nufft_internal.cuh"
 
 #include <cmath>
@@ -350,6 +354,102 @@ __global__ void __launch_bounds__(tile_threads<CONTIG>(), tile_blocks<CONTIG>())
     }
 }
 
+// 256-point passes (every axis of a 256^D grid): 16 columns per 256-thread
+// block, 16 entries per thread, the 16 x 16 decomposition with all sizes
+// fixed at compile time: entry n = t + 16 j; a 16-point DFT over j in
+// registers (index k1), the twiddle W256^(t k1) from a shared table, one
+// exchange through shared memory (padded so both sides are free of bank
+// conflicts), a 16-point DFT over t (index k2): X[k1 + 16 k2].  NIN / NOUT:
+// entries read / written per column (128 where the other half is the zero
+// padding or is cropped away).  CONTIG: the lanes run along the column (the
+// transform axis is contiguous); else across 16 adjacent columns.
+template <bool CONTIG, bool INV, int NIN, int NOUT>
+__global__ void __launch_bounds__(256) pfft256_kernel(PfftPass q, const float2* __restrict__ in,
+                                                      float2* __restrict__ out) {
+    __shared__ float2 sx[16 * 257];   // entry (k1, column, t), k1-major, 257 apart
+    __shared__ float2 stw[256];       // W256^(t k1) at [k1 16 + t]
+    {
+        const int k1 = threadIdx.x >> 4, t = threadIdx.x & 15;
+        float sn, cs;
+        sincospif(-(float)(t * k1) / 128.f, &sn, &cs);
+        stw[threadIdx.x] = make_float2(cs, INV ? -sn : sn);
+    }
+    __syncthreads();
+    const int lo = threadIdx.x & 15, hi = threadIdx.x >> 4;
+    const int t = CONTIG ? lo : hi;    // first stage: this thread's subsequence
+    const int cl = CONTIG ? hi : lo;   // its column within the tile
+    const int k1 = CONTIG ? lo : hi;   // second stage: its frequency k1
+    const int64_t per_batch = (q.ncol + 15) >> 4;
+    const int64_t ntiles = per_batch * q.nbatch;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t bt = tile / per_batch;
+        const int64_t col = ((tile - bt * per_batch) << 4) + cl;
+        const bool live = col < q.ncol;
+        float lead = 1.f;
+        if (CONTIG && (q.scale_in || q.scale_out) && live) lead = row_lead(q, (int)col);
+        float2 v[16];
+        const float2* ip = in + bt * q.in_b + col * q.in_c;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int i = t + 16 * j;
+            float2 x = make_float2(0.f, 0.f);
+            if (j < NIN / 16 && live) {
+                x = __ldg(ip + (int64_t)i * q.in_i);
+                if (CONTIG && q.scale_in) {
+                    const float sv = lead * __ldg(q.sl + i);
+                    x.x *= sv;
+                    x.y *= sv;
+                }
+            }
+            v[j] = x;
+        }
+        dftR<16>(v, 0, INV);
+#pragma unroll
+        for (int k = 1; k < 16; ++k) v[k] = cmul(v[k], stw[k * 16 + t]);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) sx[k * 257 + (CONTIG ? cl * 16 + t : t * 16 + cl)] = v[k];
+        __syncthreads();
+#pragma unroll
+        for (int tt = 0; tt < 16; ++tt) v[tt] = sx[k1 * 257 + (CONTIG ? cl * 16 + tt : tt * 16 + cl)];
+        __syncthreads();   // the next tile's writes come after every read
+        dftR<16>(v, 0, INV);
+        if (live) {
+            float2* op = out + bt * q.out_b + col * q.out_c;
+#pragma unroll
+            for (int k2 = 0; k2 < NOUT / 16; ++k2) {
+                const int o = k1 + 16 * k2;
+                float2 x = v[k2];
+                if (CONTIG) {
+                    float sc = q.norm;
+                    if (q.scale_out) {
+                        const float snv = lead * __ldg(q.sl + o);
+                        if (q.scale_out == 1) sc *= snv;
+                        x.x *= sc;
+                        x.y *= sc;
+                        if (q.scale_out == 2) {
+                            x.x /= snv;
+                            x.y /= snv;
+                        }
+                    } else {
+                        x.x *= sc;
+                        x.y *= sc;
+                    }
+                }
+                op[(int64_t)o * q.out_i] = x;
+            }
+        }
+    }
+}
+
+template <bool CONTIG, bool INV, int NIN, int NOUT>
+int run_pass256(const nufft_plan_s* p, const PfftPass& q, const float2* in, float2* out,
+                cudaStream_t s) {
+    const int64_t tiles = ((q.ncol + 15) / 16) * q.nbatch;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)p->num_sms * 4));
+    pfft256_kernel<CONTIG, INV, NIN, NOUT><<<blocks, 256, 0, s>>>(q, in, out);
+    return check_launch("pfft256_kernel");
+}
+
 int ilog2(int v) {
     int l = 0;
     while ((1 << l) < v) ++l;
@@ -421,20 +521,39 @@ int run_pass_dir(const nufft_plan_s* p, PfftPass q, const float2* in, float2* ou
 template <bool CONTIG>
 int run_pass(const nufft_plan_s* p, const PfftPass& q, const float2* in, float2* out,
              cudaStream_t s) {
+    if (q.K == 256 && (q.n_in == 128 || q.n_in == 256) && (q.n_out == 128 || q.n_out == 256)) {
+        const bool hi_in = q.n_in == 256, hi_out = q.n_out == 256;
+        if (q.inverse) {
+            if (hi_in && hi_out) return run_pass256<CONTIG, true, 256, 256>(p, q, in, out, s);
+            if (hi_in) return run_pass256<CONTIG, true, 256, 128>(p, q, in, out, s);
+            if (hi_out) return run_pass256<CONTIG, true, 128, 256>(p, q, in, out, s);
+            return run_pass256<CONTIG, true, 128, 128>(p, q, in, out, s);
+        }
+        if (hi_in && hi_out) return run_pass256<CONTIG, false, 256, 256>(p, q, in, out, s);
+        if (hi_in) return run_pass256<CONTIG, false, 256, 128>(p, q, in, out, s);
+        if (hi_out) return run_pass256<CONTIG, false, 128, 256>(p, q, in, out, s);
+        return run_pass256<CONTIG, false, 128, 128>(p, q, in, out, s);
+    }
     return q.inverse ? run_pass_dir<CONTIG, true>(p, q, in, out, s)
                      : run_pass_dir<CONTIG, false>(p, q, in, out, s);
 }
 
 }  // namespace
 
+// Own passes: asked for (NUFFT_FLAG_OWN_FFT), or by default where every pass
+// is a 256-point one (every Kd 256, every Nd 128 or 256: 3D 128^3 -> 256^3
+// xx2k 0.077 / k2xx 0.091 ms against cuFFT's 0.111 / 0.146 ms); never with
+// NUFFT_FLAG_CUFFT.
 bool pfft_eligible(const nufft_plan_s* p) {
-    if (!(p->flags & NUFFT_FLAG_OWN_FFT)) return false;
+    if (p->flags & NUFFT_FLAG_CUFFT) return false;
     if (p->B != 1 || p->ninst != 1 || p->ndim < 2) return false;
+    bool all256 = true;
     for (int d = 0; d < p->ndim; ++d) {
         const int K = p->Kd[d];
         if (K < 16 || K > 4096 || (K & (K - 1)) != 0 || p->Nd[d] > K) return false;
+        all256 = all256 && K == 256 && (p->Nd[d] == 128 || p->Nd[d] == 256);
     }
-    return true;
+    return (p->flags & NUFFT_FLAG_OWN_FFT) || all256;
 }
 
 int pfft_init(nufft_plan_s* p) {

@@ -64,7 +64,7 @@ class NUFFT:
 
     # ------------------------------------------------------------------ plan
     def plan(self, om, Nd, Kd, Jd, ft_axes=None, batch=None, deterministic=False,
-             bins=None, max_sub_points=None, autotune=False, fft='cufft'):
+             bins=None, max_sub_points=None, autotune=False, fft='auto'):
         """Plan for the points ``om`` (M x ndim radians).
 
         Argument checks follow helper.plan (src/_helper/helper.py:644-654):
@@ -73,14 +73,16 @@ class NUFFT:
         gridding mode.  ``bins``/``max_sub_points`` override the gridding bin
         shape; ``autotune=True`` applies the cached best setting for this
         geometry and point density, or searches once (``pynufft_gb300.autotune``).
-        ``fft='own'`` runs the image <-> spectrum transforms through the
+        ``fft`` picks the image <-> spectrum transform: ``'own'`` the
         library's own pruned power-of-two passes where the plan allows them
-        (one coil, 2D/3D, every Kd a power of two); the default ``'cufft'``
-        uses cuFFT, faster on this GPU.  Returns 0.
+        (one coil, 2D/3D, every Kd a power of two), ``'cufft'`` cuFFT, and the
+        default ``'auto'`` the own passes where their specialised 256-point
+        kernels apply (every Kd 256, every Nd 128 or 256: faster than cuFFT
+        on a GB300) and cuFFT elsewhere.  Returns 0.
         """
         self._check_shapes(Nd, Kd, Jd)
-        if fft not in ('cufft', 'own'):
-            raise ValueError("fft must be 'cufft' or 'own'")
+        if fft not in ('auto', 'cufft', 'own'):
+            raise ValueError("fft must be 'auto', 'cufft' or 'own'")
         ndim = len(Nd)
         if ft_axes is not None and tuple(sorted(ft_axes)) != tuple(range(ndim)):
             raise NotImplementedError('pynufft_gb300 transforms over all axes (ft_axes=None)')
@@ -131,12 +133,14 @@ class NUFFT:
                            'Nd=(256,256),Kd=(512,512),Jd=(6,6)')
 
     def _plan_common(self, oms, Nd, Kd, Jd, batch, B, ninst, deterministic, bins, max_sub,
-                     fft='cufft'):
+                     fft='auto'):
         torch = _torch()
         ndim = len(Nd)
         flags = _lib.NUFFT_FLAG_DETERMINISTIC if deterministic else 0
         if fft == 'own':
             flags |= _lib.NUFFT_FLAG_OWN_FFT
+        elif fft == 'cufft':
+            flags |= _lib.NUFFT_FLAG_CUFFT
         key = (tuple(Nd), tuple(Kd), tuple(Jd), B, ninst, flags,
                None if bins is None else tuple(bins), max_sub)
         reuse = (self._plan is not None and getattr(self, '_key', None) == key

@@ -4,8 +4,10 @@ one instance, 2D/3D, every Kd a power of two in 16..4096).
 Each case runs the image <-> spectrum stages and the transforms built on them
 against the oracle (numpy fftn / ifftn, the reference's xx2k / k2xx,
 nufft/_nufft_class_methods_cpu.py:232-249, 316-329) and against the same plan
-run through cuFFT (the default).  The passes are opt-in (``fft='own'``,
-NUFFT_FLAG_OWN_FFT).  Bound: 1e-5 relative L2 (float32 passes land near 1e-7).
+run through cuFFT.  The passes are chosen by default where their 256-point
+kernels apply (every Kd 256, every Nd 128 or 256), else on request
+(``fft='own'``, NUFFT_FLAG_OWN_FFT).  Bound: 1e-5 relative L2 (float32
+passes land near 1e-7).
 """
 import ctypes
 
@@ -24,6 +26,9 @@ CASES = [
     ((16, 16, 16), (32, 32, 32), (6, 6, 6)),
     ((8, 12, 24), (16, 32, 64), (4, 6, 6)),       # the smallest K, anisotropic
     ((20, 24, 12), (32, 64, 16), (6, 6, 4)),      # Nd above Kd / 2 on two axes
+    ((128, 128), (256, 256), (6, 6)),             # the 256-point passes, half the inputs
+    ((128, 256), (256, 256), (6, 6)),             # 256-point passes with every input
+    ((40, 128, 100), (64, 256, 256), (6, 6, 6)),  # 256-point and general passes mixed
 ]
 
 
@@ -55,7 +60,7 @@ def test_own_pruned_fft_matches_oracle_and_cufft(NUFFT, Nd, Kd, Jd):
     A.plan(om, Nd, Kd, Jd, fft='own')
     assert kind(A) == _lib.NUFFT_FFT_OWN_PRUNED
     C = NUFFT(0)
-    C.plan(om, Nd, Kd, Jd)
+    C.plan(om, Nd, Kd, Jd, fft='cufft')
     assert kind(C) == _lib.NUFFT_FFT_CUFFT_PRUNED
     O = OracleNUFFT()
     O.plan(om, Nd, Kd, Jd)
@@ -97,3 +102,19 @@ def test_fft_option_is_checked(NUFFT):
     A = NUFFT(0)
     with pytest.raises(ValueError):
         A.plan(np.zeros((4, 2)), (8, 8), (16, 16), (4, 4), fft='fftw')
+
+
+def test_default_transform_choice(NUFFT):
+    """Without a choice the plan runs the own passes where every Kd is 256 and
+    every Nd 128 or 256, cuFFT elsewhere; fft='cufft' forces cuFFT."""
+    from pynufft_gb300 import _lib
+    om = np.random.default_rng(3).uniform(-np.pi, np.pi, (500, 2))
+    for Nd, Kd, want in [((128, 128), (256, 256), _lib.NUFFT_FFT_OWN_PRUNED),
+                         ((128, 256), (256, 256), _lib.NUFFT_FFT_OWN_PRUNED),
+                         ((100, 128), (256, 256), _lib.NUFFT_FFT_CUFFT_PRUNED),
+                         ((256, 256), (512, 512), _lib.NUFFT_FFT_CUFFT_PRUNED)]:
+        A = NUFFT(0)
+        A.plan(om, Nd, Kd, (6, 6))
+        assert kind(A) == want, (Nd, Kd)
+        A.plan(om, Nd, Kd, (6, 6), fft='cufft')
+        assert kind(A) == _lib.NUFFT_FFT_CUFFT_PRUNED
