@@ -364,8 +364,8 @@ __global__ void __launch_bounds__(tile_threads<CONTIG>(), tile_blocks<CONTIG>())
 // padding or is cropped away).  CONTIG: the lanes run along the column (the
 // transform axis is contiguous); else across 16 adjacent columns.
 template <bool CONTIG, bool INV, int NIN, int NOUT>
-__global__ void __launch_bounds__(256) pfft256_kernel(PfftPass q, const float2* __restrict__ in,
-                                                      float2* __restrict__ out) {
+__device__ __forceinline__ void pfft256_body(const PfftPass& q, const float2* __restrict__ in,
+                                             float2* __restrict__ out) {
     __shared__ float2 sx[16 * 257];   // entry (k1, column, t), k1-major, 257 apart
     __shared__ float2 stw[256];       // W256^(t k1) at [k1 16 + t]
     {
@@ -441,13 +441,30 @@ __global__ void __launch_bounds__(256) pfft256_kernel(PfftPass q, const float2* 
     }
 }
 
+// Passes reading every entry hold four blocks per SM with a 64-register cap
+// (256^3 inverse 0.092 -> 0.078 ms); the half-input passes fit four blocks
+// without it and spill under it (forward 0.077 -> 0.083 ms).
+template <bool CONTIG, bool INV, int NOUT>
+__global__ void __launch_bounds__(256) pfft256_half_kernel(PfftPass q, const float2* __restrict__ in,
+                                                           float2* __restrict__ out) {
+    pfft256_body<CONTIG, INV, 128, NOUT>(q, in, out);
+}
+template <bool CONTIG, bool INV, int NOUT>
+__global__ void __launch_bounds__(256, 4) pfft256_full_kernel(PfftPass q, const float2* __restrict__ in,
+                                                              float2* __restrict__ out) {
+    pfft256_body<CONTIG, INV, 256, NOUT>(q, in, out);
+}
+
 template <bool CONTIG, bool INV, int NIN, int NOUT>
 int run_pass256(const nufft_plan_s* p, const PfftPass& q, const float2* in, float2* out,
                 cudaStream_t s) {
     const int64_t tiles = ((q.ncol + 15) / 16) * q.nbatch;
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)p->num_sms * 4));
-    pfft256_kernel<CONTIG, INV, NIN, NOUT><<<blocks, 256, 0, s>>>(q, in, out);
-    return check_launch("pfft256_kernel");
+    if constexpr (NIN == 256)
+        pfft256_full_kernel<CONTIG, INV, NOUT><<<blocks, 256, 0, s>>>(q, in, out);
+    else
+        pfft256_half_kernel<CONTIG, INV, NOUT><<<blocks, 256, 0, s>>>(q, in, out);
+    return check_launch("pfft256 pass");
 }
 
 int ilog2(int v) {
