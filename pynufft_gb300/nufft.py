@@ -448,8 +448,9 @@ class NUFFT:
                                      f'tensor of shape {self._shape(kout)}')
         dev = self.device
         comp = torch.cuda.current_stream(dev)
-        up = torch.cuda.Stream(dev)
-        down = torch.cuda.Stream(dev)
+        if getattr(self, '_copy_streams', None) is None:   # made once per operator
+            self._copy_streams = (torch.cuda.Stream(dev), torch.cuda.Stream(dev))
+        up, down = self._copy_streams
         bufs = {}
         freed_in = [None] * depth     # compute of the slot's last job done
         freed_out = [None] * depth    # download of the slot's last result done
