@@ -13,7 +13,9 @@ Prints ONE JSON line (rank 0).  `value` times steps with inputs resident on
 the device (CUDA events on the launching stream); `e2e` times the public API
 on pinned host tensors, every step's copies in and out included
 (`NUFFT.run_many`, which overlaps one step's copies with the neighbouring
-steps' transforms; `e2e_sync`: `NUFFT.forward`/`adjoint` one call at a time);
+steps' transforms and, on workloads whose step takes 0.1 ms or more on the
+device, runs alternate jobs on a twin operator of the same points on a
+second stream; `e2e_sync`: `NUFFT.forward`/`adjoint` one call at a time);
 `roofline` uses the dominant kernel's own average duration, from CUDA events
 that the library records around every n-th of its launches (about 20 spread
 over the timed steps) on the launching stream;
@@ -423,6 +425,10 @@ def main():
                     help='print only the multi-coil leg (a development aid; not a bench line)')
     ap.add_argument('--deterministic', action='store_true',
                     help='plan the workload in the deterministic gridding mode')
+    ap.add_argument('--lanes', type=int, default=0,
+                    help='concurrent lanes of the end-to-end leg (NUFFT.run_many); '
+                         '0: two when a step takes 0.1 ms or more on the device, else one '
+                         '(shorter steps are bound by the host issuing them)')
     ap.add_argument('--fft', default='auto', choices=['auto', 'cufft', 'own'],
                     help="the plan's image <-> spectrum transform (auto: the library's choice; "
                          "own: its pruned passes, one-coil power-of-two plans; cufft)")
@@ -601,7 +607,9 @@ def main():
     # end to end through the public API, pinned host buffers, copies included:
     # every step copies its image and its samples in and both results out.
     # `run_many` keeps the host link busy while the GPU transforms (the
-    # copies of one step overlap the neighbouring steps' transforms);
+    # copies of one step overlap the neighbouring steps' transforms) and
+    # runs consecutive steps on `--lanes` operators of the same points, one
+    # stream each, so that independent steps' kernels overlap on the GPU;
     # `e2e_sync` calls forward() and adjoint() one at a time, each returning
     # its host result before the next starts.
     xh = torch.from_numpy(x).pin_memory()
@@ -618,10 +626,11 @@ def main():
     t_sync = (time.perf_counter() - t0) / e2e_steps / ninst
     jobs = [j for _ in range(e2e_steps) for j in (('forward', xh), ('adjoint', yh))]
     outs = [torch.empty_like(xh if name == 'adjoint' else yh).pin_memory() for name, _ in jobs]
-    A.run_many(jobs, out=outs)           # warm-up (streams, device buffers)
+    lanes = args.lanes if args.lanes > 0 else (2 if ms_per_step >= 0.1 else 1)
+    A.run_many(jobs, out=outs, lanes=lanes)   # warm-up (twins, streams, device buffers)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    A.run_many(jobs, out=outs)
+    A.run_many(jobs, out=outs, lanes=lanes)
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / e2e_steps / ninst
     if dist:
@@ -663,7 +672,8 @@ def main():
                        'frac': nbytes / (t_k2y / 1e3) / 1e9 / peak},
             'cpu_baseline': cpu,
             'e2e': {'value': world / t_e2e, 'unit': 'pairs/s', 'h2d_bytes_per_step': h2d,
-                    'd2h_bytes_per_step': d2h, 'api': 'NUFFT.run_many', 'steps': e2e_steps},
+                    'd2h_bytes_per_step': d2h, 'api': 'NUFFT.run_many', 'steps': e2e_steps,
+                    'lanes': lanes},
             'e2e_sync': {'value': world / t_sync, 'unit': 'pairs/s',
                          'api': 'NUFFT.forward + NUFFT.adjoint, one call at a time'},
             'gpu_launches': launches_per_step * args.steps,

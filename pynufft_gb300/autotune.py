@@ -112,7 +112,7 @@ def _replan(op, oms, bins, msub):
                      bins=bins, max_sub_points=msub)
     else:
         op.plan(oms[0], op.Nd, op.Kd, op.Jd, batch=op.batch, deterministic=det,
-                bins=bins, max_sub_points=msub)
+                bins=bins, max_sub_points=msub, fft=getattr(op, 'fft', 'auto'))
 
 
 def apply(op, oms, choice):

@@ -60,6 +60,10 @@ class NUFFT:
         self.batch = None
         self.ninst = 1
         self._plan = None
+        self._points = None
+        self._twins = []
+        self._lane_streams = []
+        self.fft = 'auto'
         self._lib = _lib.load()
 
     # ------------------------------------------------------------------ plan
@@ -186,6 +190,9 @@ class NUFFT:
             _lib.check(self._lib.nufft_set_points(h, cnt, c_void_p(ptr), 1 if on_dev else 0,
                                                   self._stream()), 'plan')
             self._key = key
+            self._points = (om_all, tuple(counts))   # a copy, for run_many's twin plans
+            self._drop_twins()
+        self.fft = fft
         self.Nd, self.Kd, self.Jd = tuple(Nd), tuple(Kd), tuple(Jd)
         self.ndims = ndim
         self.ft_axes = tuple(range(ndim))
@@ -236,11 +243,37 @@ class NUFFT:
 
     def release(self):
         """Free the plan's device memory (nufft/_nufft_class_methods_device.py:653-683)."""
+        self._drop_twins()
         if getattr(self, '_plan', None) is not None:
             self._lib.nufft_plan_destroy(self._plan)
             self._plan = None
         self._key = None
         self._maps = None
+        self._points = None
+
+    def _drop_twins(self):
+        for t in getattr(self, '_twins', None) or ():
+            t.release()
+        self._twins = []
+
+    def _twin(self):
+        """Another operator with this one's points and settings and its own
+        device buffers, so that a second stream can transform at the same
+        time (run_many's lanes)."""
+        torch = _torch()
+        om_all, counts = self._points
+        Nd, Kd, Jd, B, ninst, flags, bins, max_sub = self._key
+        if isinstance(om_all, torch.Tensor):
+            oms = list(torch.split(om_all, list(counts)))
+        else:
+            oms = numpy.split(om_all, numpy.cumsum(counts)[:-1])
+        t = NUFFT(self.device)
+        t._plan_common(oms, Nd, Kd, Jd, self.batch, B, ninst,
+                       bool(flags & _lib.NUFFT_FLAG_DETERMINISTIC), bins, max_sub, self.fft)
+        k2y, y2k = getattr(self, 'methods', (None, None))
+        if k2y is not None or y2k is not None:
+            t.set_methods(k2y, y2k)
+        return t
 
     def __del__(self):
         try:
@@ -259,6 +292,7 @@ class NUFFT:
         ym = 0 if y2k is None else self.Y2K_METHODS[y2k]
         _lib.check(self._lib.nufft_plan_set_methods(self._plan, km, ym), 'set_methods')
         self.methods = (k2y, y2k)
+        self._drop_twins()
 
     def check(self):
         """Synchronise the plan's stream and raise NufftError if a kernel gave up
@@ -401,7 +435,7 @@ class NUFFT:
                'x2xx': ('x', 'x'), 'xx2x': ('x', 'x'), 'xx2k': ('x', 'k'), 'k2xx': ('k', 'x'),
                'k2y': ('k', 'y'), 'y2k': ('y', 'k'), 'k2y2k': ('k', 'k')}
 
-    def run_many(self, jobs, depth=2, out=None):
+    def run_many(self, jobs, depth=2, out=None, lanes=1):
         """Apply a sequence of operators to host arrays, with the host link
         busy while the GPU transforms.
 
@@ -413,15 +447,22 @@ class NUFFT:
         current stream, and results are copied back on a download stream
         into pinned CPU tensors, so the copies of job i+1's input and job
         i-1's result overlap job i's transform; `depth` jobs' device buffers
-        rotate.  Returns the results in order (written into `out`, a list of
-        pinned complex64 CPU tensors of the results' shapes, when given).
-        Each result equals that of calling the method alone.
+        rotate.  With ``lanes`` = L > 1, job i runs on lane i mod L: lane 0
+        is this operator on the current stream, the others are twin
+        operators of the same points (made on first use and kept; each holds
+        its own plan tables and scratch) on streams of their own, so that
+        the transforms of independent jobs overlap on the GPU.  Returns the
+        results in order (written into `out`, a list of pinned complex64
+        CPU tensors of the results' shapes, when given).  Each result equals
+        that of calling the method alone (bitwise on deterministic plans).
         """
         torch = _torch()
         if self._plan is None:
             raise RuntimeError('plan() has not been called')
         if depth < 1:
             raise ValueError('depth must be at least 1')
+        if lanes < 1:
+            raise ValueError('lanes must be at least 1')
         todo = []
         for name, a in jobs:
             if name not in self._STAGES:
@@ -446,18 +487,29 @@ class NUFFT:
                         or tuple(o.shape) != self._shape(kout)):
                     raise ValueError(f'out: {name} needs a pinned contiguous complex64 CPU '
                                      f'tensor of shape {self._shape(kout)}')
+        lanes = max(1, min(lanes, len(todo)))
         dev = self.device
         comp = torch.cuda.current_stream(dev)
         if getattr(self, '_copy_streams', None) is None:   # made once per operator
             self._copy_streams = (torch.cuda.Stream(dev), torch.cuda.Stream(dev))
         up, down = self._copy_streams
-        bufs = {}
-        freed_in = [None] * depth     # compute of the slot's last job done
-        freed_out = [None] * depth    # download of the slot's last result done
-        outs = []
         with torch.cuda.device(dev):
+            while len(self._twins) < lanes - 1:
+                self._twins.append(self._twin())
+            if len(self._lane_streams) < lanes - 1:
+                self._lane_streams = [torch.cuda.Stream(dev) for _ in range(lanes - 1)]
+            ops = [self] + self._twins[:lanes - 1]
+            streams = [comp] + self._lane_streams[:lanes - 1]
+            for s in streams[1:]:
+                s.wait_stream(comp)
+            bufs = {}
+            freed_in = {}     # compute of the (lane, slot)'s last job done
+            freed_out = {}    # download of the (lane, slot)'s last result done
+            outs = []
             for i, (name, h, kin, kout) in enumerate(todo):
-                s = i % depth
+                ln = i % lanes
+                s = (ln, (i // lanes) % depth)
+                cs = streams[ln]
                 din = bufs.get((s, 'in', kin))
                 if din is None:
                     din = bufs[(s, 'in', kin)] = self._empty(kin)
@@ -465,19 +517,19 @@ class NUFFT:
                 if dout is None:
                     dout = bufs[(s, 'out', kout)] = self._empty(kout)
                 with torch.cuda.stream(up):
-                    if freed_in[s] is not None:
+                    if s in freed_in:
                         up.wait_event(freed_in[s])
                     din.copy_(h, non_blocking=True)
                     ev_up = torch.cuda.Event()
                     ev_up.record(up)
-                comp.wait_event(ev_up)
-                if freed_out[s] is not None:
-                    comp.wait_event(freed_out[s])
+                cs.wait_event(ev_up)
+                if s in freed_out:
+                    cs.wait_event(freed_out[s])
                 fn = getattr(self._lib, 'nufft_' + name)
-                _lib.check(fn(self._plan, c_void_p(din.data_ptr()), c_void_p(dout.data_ptr()),
-                              c_void_p(comp.cuda_stream)), name)
+                _lib.check(fn(ops[ln]._plan, c_void_p(din.data_ptr()), c_void_p(dout.data_ptr()),
+                              c_void_p(cs.cuda_stream)), name)
                 ev_comp = torch.cuda.Event()
-                ev_comp.record(comp)
+                ev_comp.record(cs)
                 freed_in[s] = ev_comp
                 o = (out[i] if out is not None else
                      torch.empty(self._shape(kout), dtype=torch.complex64, pin_memory=True))
@@ -490,6 +542,8 @@ class NUFFT:
                 outs.append(o)
             down.synchronize()
             comp.wait_stream(up)      # the buffers die with this call
+            for s in streams[1:]:
+                comp.wait_stream(s)
         return outs
 
     # ---- single-image FFT stages (nufft/_nufft_class_methods_cpu.py:251-264, 332-344)

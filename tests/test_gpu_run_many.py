@@ -36,12 +36,14 @@ def _jobs(A, rng, torch, n=3):
     return jobs
 
 
-@pytest.mark.parametrize('B,ndim,depth', [(None, 2, 2), (4, 2, 1), (8, 3, 3), (None, 3, 2)])
-def test_run_many_equals_single_calls_bitwise(B, ndim, depth):
+@pytest.mark.parametrize('B,ndim,depth,lanes', [(None, 2, 2, 1), (4, 2, 1, 2), (8, 3, 3, 1),
+                                                (8, 3, 2, 3), (None, 3, 2, 2)])
+def test_run_many_equals_single_calls_bitwise(B, ndim, depth, lanes):
     import torch
     A, rng = _plan(B, ndim, True)
     jobs = _jobs(A, rng, torch)
-    outs = A.run_many(jobs, depth=depth)
+    outs = A.run_many(jobs, depth=depth, lanes=lanes)
+    assert len(A._twins) == lanes - 1
     assert len(outs) == len(jobs)
     for (name, a), o in zip(jobs, outs):
         assert o.is_pinned() and o.dtype == torch.complex64
@@ -49,13 +51,14 @@ def test_run_many_equals_single_calls_bitwise(B, ndim, depth):
         assert np.array_equal(o.numpy(), ref), name
 
 
-def test_run_many_fast_plan_and_out_buffers():
+@pytest.mark.parametrize('lanes', [1, 2])
+def test_run_many_fast_plan_and_out_buffers(lanes):
     import torch
     A, rng = _plan(None, 3, False, M=20000)
     jobs = _jobs(A, rng, torch, n=6)
     out = [torch.empty(A._shape(A._STAGES[n][1]), dtype=torch.complex64).pin_memory()
            for n, _ in jobs]
-    got = A.run_many(jobs, out=out)
+    got = A.run_many(jobs, out=out, lanes=lanes)
     assert all(g is o for g, o in zip(got, out))
     for (name, a), o in zip(jobs, out):
         ref = np.asarray(getattr(A, name)(a))
@@ -76,3 +79,37 @@ def test_run_many_rejects_bad_jobs():
         A.run_many([('forward', x)], out=[torch.empty(3, dtype=torch.complex64)])
     with pytest.raises(ValueError):
         A.run_many([('forward', x)], depth=0)
+    with pytest.raises(ValueError):
+        A.run_many([('forward', x)], lanes=0)
+
+
+def test_run_many_lanes_follow_the_plan():
+    """Twin operators take the plan's points, instances, bins and transform
+    choice, and are dropped when the points or the methods change."""
+    import torch
+    from pynufft_gb300 import NUFFT
+    rng = np.random.default_rng(5)
+    oms = [rng.uniform(-np.pi, np.pi, (m, 2)) for m in (700, 1300, 400)]
+    A = NUFFT(0)
+    A.plan_many(oms, (32, 32), (64, 64), (6, 6), batch=2, deterministic=True,
+                bins=(8, 16))
+    xs = [cplx(rng, A._shape('x')) for _ in range(4)]
+    jobs = [('forward', x) for x in xs] + [('selfadjoint', x) for x in xs]
+    outs = A.run_many(jobs, lanes=2)
+    assert len(A._twins) == 1 and A._twins[0]._key == A._key
+    for (name, a), o in zip(jobs, outs):
+        assert np.array_equal(o.numpy(), np.asarray(getattr(A, name)(a))), name
+    om2 = rng.uniform(-np.pi, np.pi, (900, 2))
+    B = NUFFT(0)
+    B.plan(om2, (32, 32), (64, 64), (6, 6), deterministic=True, fft='own')
+    x = cplx(rng, B._shape('x'))
+    got = B.run_many([('forward', x), ('forward', x), ('adjoint', np.asarray(B.forward(x)))],
+                     lanes=2)
+    assert B._twins[0].fft == 'own'
+    assert np.array_equal(got[0].numpy(), got[1].numpy())
+    assert np.array_equal(got[1].numpy(), np.asarray(B.forward(x)))
+    B.plan(rng.uniform(-np.pi, np.pi, (500, 2)), (32, 32), (64, 64), (6, 6),
+           deterministic=True, fft='own')
+    assert B._twins == []
+    got = B.run_many([('forward', x), ('forward', x)], lanes=2)
+    assert got[0].shape == (500,) and np.array_equal(got[1].numpy(), np.asarray(B.forward(x)))
