@@ -216,10 +216,9 @@ bool cm_path(const nufft_plan_s* p) {
     // rows of 16 cells (bins x group along the innermost axis), not wrapping onto themselves
     if (p->bs[DI] * p->rgroup != 16 || 16 + J - 1 > p->Kd[DI]) return false;
     const int nkey = p->bs[0] * (p->ndim == 3 ? p->bs[1] : 1);
-    // (the fast kernel's shared memory, the larger: the same answer for
-    // plans of either mode)
+    // (both modes' kernels take the same shared memory)
     return nkey <= 256 && rows_smem(p->ndim, J, nkey, row_sub_cap(p->ndim), 8,
-                                    cm_row_coils(p->B), false) <= 200 * 1024;
+                                    cm_row_coils(p->B)) <= 200 * 1024;
 }
 
 // Deterministic row gridding into the coil-major spectra grid_cm: per-row

@@ -530,6 +530,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     return false;
 }
 
+// Asynchronous global -> shared copies (cp.async) of 16 or 8 bytes, both
+// addresses aligned to the size; cp_async_wait_all waits for the calling
+// thread's copies (a barrier then makes every thread's visible).
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 template <int DIM>
 __device__ __forceinline__ int tile_addr(const int (&t)[3], const TileStrides& ts) {
     if constexpr (DIM == 3) return t[0] * ts.sx + t[1] * ts.sy + t[2];

@@ -14,8 +14,11 @@
 // accumulators per lane) and visits, in a fixed order, every point whose
 // footprint crosses those rows: u = y conj(c_x c_y) for its row, then the J
 // innermost taps acc[pz + k] += u conj(c_z[k]) at register indices chosen by
-// a warp-uniform switch on pz.  The points' coefficients and offsets are
-// staged in shared memory first, sorted by row.  No shared-memory atomics
+// a warp-uniform switch on pz.  The points' coefficients and samples (a
+// coil chunk at a time) are staged in shared memory by asynchronous copies
+// (cp.async) in point order, which land while the block sorts its points by
+// row; the visits follow the row order through a packed (offsets, point
+// index) list.  No shared-memory atomics
 // and no float-to-integer conversions per tap; each lane's row is flushed
 // once per row block: float2 atomics into the grid (fast mode), or 64-bit
 // fixed-point integer atomics (deterministic mode: the per-row float sums
@@ -125,24 +128,28 @@ __device__ void sort_rows(int P, int nkey, KeyFn key, int* __restrict__ wcnt,
 
 // Shared memory of y2k_rows_kernel (bytes), for nkey row keys, at most P
 // points and a block of nwarps warps: the staged per-point data
-// (coefficients, packed tile offsets, sample index) and the row sort's
-// histogram, offsets and list.
-__host__ __device__ inline size_t rows_smem(int DIM, int JM, int nkey, int P, int nwarps, int CB,
-                                            bool DET) {
-    const size_t ints = sizeof(int) * ((size_t)2 * P + (size_t)nwarps * nkey + nkey + 1 + P);
-    const size_t sy = (DIM == 3 || !DET) ? sizeof(float2) * (size_t)P * CB + 16 : 0;
+// (coefficients, tile offsets in point order and packed in row order,
+// sample index) and the row sort's histogram, offsets and list.
+__host__ __device__ inline size_t rows_smem(int DIM, int JM, int nkey, int P, int nwarps, int CB) {
+    const size_t ints = sizeof(int) * ((size_t)3 * P + (size_t)nwarps * nkey + nkey + 1 + P);
+    const size_t sy = sizeof(float2) * (size_t)P * CB + 16;
     return sizeof(float2) * (size_t)P * DIM * JM + ints + 16 + sy;
 }
 
 // Row gridding.  One block per row sub-problem: up to g.rgroup consecutive
 // bins along the innermost axis (3D), at most row_sub_cap points; the tile is
 // (bs0 + J - 1) x (bs1 + J - 1) rows of TZ = rgroup * bs_z + J - 1 cells.
+// 3D: at most 80 registers, three blocks per SM (8-coil kooshball adjoint
+// 11.0 -> 9.6 ms fast, 13.3 -> 11.9 ms deterministic); 2D: no minimum (0),
+// the compiler's choice of ~80 registers ran faster than the same bound.
 template <int DIM, int JM, int TZ, int CB, bool DET>
-__global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __restrict__ y,
+__global__ void __launch_bounds__(256, (DIM == 3) ? 3 : 0) y2k_rows_kernel(Geom g, const float2* __restrict__ y,
                                                        float2* __restrict__ grid,
                                                        unsigned long long* __restrict__ igrid,
                                                        const double* __restrict__ dscal) {
     static_assert(DIM == 2 || DIM == 3, "rows of a 2D or 3D tile");
+    static_assert(JM % 2 == 0, "coefficient rows staged in 16-byte pieces");
+    static_assert(TZ <= 64, "tap offset packed in 6 bits");
     using RSl = RowSlots<DIM, CB>;
     constexpr int RS0 = RSl::RS0, RS1 = RSl::RS1;
     constexpr int DI = DIM - 1;
@@ -155,44 +162,75 @@ __global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __r
     const int bs0 = g.bs[0], bs1 = (DIM == 3) ? g.bs[1] : 1;
     const int nkey = bs0 * bs1;
     const int nwarps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr bool STAGEY = (DIM == 3 || !DET);   // samples staged in shared memory
     constexpr int PCAP = (DIM == 2) ? kRowSub2 : kRowSub3;   // points per sub-problem at most
-    float2* scoef = reinterpret_cast<float2*>(smem_raw);                 // PCAP x DIM x JM
-    int* sinfo = reinterpret_cast<int*>(scoef + (size_t)PCAP * PC);      // pz | lx << 8 | ly << 16
-    int* sm = sinfo + PCAP;                                              // sample index
-    int* wcnt = sm + PCAP;
+    static_assert(PCAP <= 1024, "point index packed in 10 bits");
+    float2* scoef = reinterpret_cast<float2*>(smem_raw);                 // PCAP x DIM x JM, point order
+    int* sinfo = reinterpret_cast<int*>(scoef + (size_t)PCAP * PC);      // row order, packed
+    int* sm = sinfo + PCAP;                // sample index, point order
+    int* sraw = sm + PCAP;                 // point order: pz | lx << 6 | ly << 14
+    int* wcnt = sraw + PCAP;
     int* off = wcnt + nwarps * nkey;
     int* list = off + nkey + 1;
-    // STAGEY: the samples of the current coil chunk, PCAP x CB, 16-byte aligned
+    // the samples of the current coil chunk, PCAP x CB in point order,
+    // 16-byte aligned
     float2* sy = reinterpret_cast<float2*>(
         (reinterpret_cast<uintptr_t>(list + PCAP) + 15) & ~static_cast<uintptr_t>(15));
+    const int B = g.B;
+    const bool y16 = (reinterpret_cast<uintptr_t>(y) & 15) == 0;
+    // the samples of coils [b0, b0 + CB) of every point, by asynchronous copies
+    auto stage_samples = [&](int b0) {
+        if (y16) {
+            constexpr int H = CB / 2;
+            for (int e = threadIdx.x; e < P * H; e += blockDim.x) {
+                const int i = e / H, c = 2 * (e - i * H);
+                cp_async16(sy + i * CB + c, y + (size_t)sm[i] * B + b0 + c);
+            }
+        } else {
+            for (int e = threadIdx.x; e < P * CB; e += blockDim.x) {
+                const int i = e / CB, c = e - i * CB;
+                cp_async8(sy + e, y + (size_t)sm[i] * B + b0 + c);
+            }
+        }
+    };
 
     const int* __restrict__ pos0 = g.pos[0];
     const int* __restrict__ pos1 = g.pos[DIM == 3 ? 1 : 0];
-    auto key = [&](int i) {
+    // per point (point order): tile offsets, sample index; the coefficients
+    // (consecutive points' rows are contiguous) and the first coil chunk's
+    // samples start copying asynchronously and land during the row sort
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
         const int s = sp.y + i;
-        const int lx = __ldg(pos0 + s) - o[0];
-        if constexpr (DIM == 3) return lx * bs1 + (__ldg(pos1 + s) - o[1]);
-        return lx;
-    };
-    sort_rows(P, nkey, key, wcnt, off, list);
-    // stage the points in row order: coefficients, offsets in the tile, sample
-    for (int e = threadIdx.x; e < P * PC; e += blockDim.x) {
-        const int j = e / PC, r = e - j * PC, d = r / JM, k = r - d * JM;
-        const int s = sp.y + list[j];
-        scoef[e] = __ldg(g.coef[d] + (size_t)s * g.JP[d] + k);
-    }
-    for (int j = threadIdx.x; j < P; j += blockDim.x) {
-        const int s = sp.y + list[j];
         const int lx = __ldg(pos0 + s) - o[0];
         const int ly = (DIM == 3) ? __ldg(pos1 + s) - o[1] : 0;
         const int pz = __ldg(g.pos[DI] + s) - o[DI];
-        sinfo[j] = pz | (lx << 8) | (ly << 16);
-        sm[j] = __ldg(g.perm + s);
+        sraw[i] = pz | (lx << 6) | (ly << 14);
+        sm[i] = __ldg(g.perm + s);
+    }
+    {
+        constexpr int CQ = JM / 2;   // 16-byte pieces of one axis's coefficients
+        for (int e = threadIdx.x; e < P * DIM * CQ; e += blockDim.x) {
+            const int i = e / (DIM * CQ), r = e - i * (DIM * CQ), d = r / CQ, q = r - d * CQ;
+            cp_async16(scoef + (size_t)i * PC + d * JM + 2 * q,
+                       g.coef[d] + (size_t)(sp.y + i) * g.JP[d] + 2 * q);
+        }
     }
     __syncthreads();
+    stage_samples(0);
+    auto key = [&](int i) {
+        const int r = sraw[i];
+        const int lx = (r >> 6) & 255;
+        if constexpr (DIM == 3) return lx * bs1 + ((r >> 14) & 255);
+        return lx;
+    };
+    sort_rows(P, nkey, key, wcnt, off, list);
+    // row order: packed offsets and the point index
+    for (int j = threadIdx.x; j < P; j += blockDim.x) {
+        const int i = list[j];
+        sinfo[j] = sraw[i] | (i << 22);
+    }
+    cp_async_wait_all();
+    __syncthreads();
 
-    const int B = g.B;
     const int T0 = g.T[0], T1 = (DIM == 3) ? g.T[1] : 1;
     const int nrb0 = (T0 + RS0 - 1) / RS0, nrb1 = (T1 + RS1 - 1) / RS1;
     const int nrb = nrb0 * nrb1;
@@ -225,13 +263,10 @@ __global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __r
         }
     };
     for (int b0 = 0; b0 < B; b0 += CB) {
-        const float2* __restrict__ yc = y + b0 + b;
-        if constexpr (STAGEY) {   // this chunk's samples, coalesced over the coils
+        if (b0 > 0) {   // the next chunk's samples (the first came with the sort)
             __syncthreads();        // the previous chunk's samples are read
-            for (int e = threadIdx.x; e < P * CB; e += blockDim.x) {
-                const int j = e / CB, c = e - j * CB;
-                sy[e] = __ldg(y + (size_t)sm[j] * B + b0 + c);
-            }
+            stage_samples(b0);
+            cp_async_wait_all();
             __syncthreads();
         }
         if (DIM == 3) {
@@ -253,20 +288,14 @@ __global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __r
                 if (j0 >= j1) continue;
                 touched = true;
                 const int ix = R0 + gx - lx;
-                float2 ynext = STAGEY ? make_float2(0.f, 0.f) : __ldg(yc + (size_t)sm[j0] * B);
                 for (int j = j0; j < j1; ++j) {
-                    float2 yv;
-                    if constexpr (STAGEY) {
-                        yv = sy[j * CB + b];
-                    } else {
-                        yv = ynext;
-                        if (j + 1 < j1) ynext = __ldg(yc + (size_t)sm[j + 1] * B);
-                    }
                     const int info = sinfo[j];
-                    const float2* cj = scoef + (size_t)j * PC;
+                    const int pi = info >> 22;   // the point's index in the sub-problem
+                    const float2 yv = sy[pi * CB + b];
+                    const float2* cj = scoef + (size_t)pi * PC;
                     float2 w = make_float2(0.f, 0.f);
                     if constexpr (DIM == 3) {
-                        const int iy = R1 + gy - (info >> 16);
+                        const int iy = R1 + gy - ((info >> 14) & 255);
                         if (ix >= 0 && ix < JM && iy >= 0 && iy < JM) w = cmul(cj[ix], cj[JM + iy]);
                     } else {
                         if (ix >= 0 && ix < JM) w = cj[ix];
@@ -274,7 +303,7 @@ __global__ void __launch_bounds__(256) y2k_rows_kernel(Geom g, const float2* __r
                     float2 cz[JM];
 #pragma unroll
                     for (int k = 0; k < JM; ++k) cz[k] = cj[DI * JM + k];
-                    row_taps_at<TZ, JM>(info & 255, acc, cmulc(yv, w), cz);
+                    row_taps_at<TZ, JM>(info & 63, acc, cmulc(yv, w), cz);
                 }
             }
             if (!touched) continue;   // warp-uniform: no point crosses these rows

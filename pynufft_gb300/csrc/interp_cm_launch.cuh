@@ -21,7 +21,7 @@ static int y2k_rows_launch(const Geom& g, const float2* y, float2* grid, unsigne
     auto kern = y2k_rows_kernel<DIM, JM, TZ, CB, DET>;
     const int threads = 256;
     const int nkey = g.bs[0] * (DIM == 3 ? g.bs[1] : 1);
-    const size_t smem = rows_smem(DIM, JM, nkey, row_sub_cap(DIM), threads / 32, CB, DET);
+    const size_t smem = rows_smem(DIM, JM, nkey, row_sub_cap(DIM), threads / 32, CB);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);

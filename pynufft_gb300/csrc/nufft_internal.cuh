@@ -32,13 +32,14 @@ constexpr int kGatherSub = 512;
 // row_sub_cap points, so the tile's halo along that axis is shared.
 constexpr int kRowGroup = 4;
 // Row sub-problems hold at most kRowSub2 (2D) / kRowSub3 (3D) points, so
-// that the row kernels can stage their samples (all coils of a lane group)
-// in shared memory as well, two blocks per SM: 32-coil radial adjoint 0.447
-// -> 0.424 ms; 8-coil kooshball 21.2 -> 20.2 ms deterministic, 16.4 -> 15.5
-// ms fast.  The 2D deterministic kernel does not stage (0.97 against 1.00
-// ms) but keeps the same lists, so both modes' plans hold the same tables.
-constexpr int kRowSub2 = 256;
-constexpr int kRowSub3 = 448;
+// that the row kernels stage their coefficients and samples (all coils of a
+// lane group) in shared memory three blocks per SM (8 coils in 3D, 32 in
+// 2D): 32-coil radial adjoint 0.219 ms with 256 points (two blocks) against
+// 0.200 ms; 8-coil kooshball with 448 points 11.0 ms fast against 9.6 ms
+// with 320.  Both modes use the same lists, so their plans hold the same
+// tables (and the deterministic sums do not depend on the plan's mode).
+constexpr int kRowSub2 = 192;
+constexpr int kRowSub3 = 320;
 inline int row_sub_cap(int ndim) { return ndim == 2 ? kRowSub2 : kRowSub3; }
 
 void set_error(const std::string& msg);
