@@ -549,6 +549,10 @@ def main():
     lib.nufft_plan_transform_kind(A._plan, byref(fkind))
     if fkind.value == _lib.NUFFT_FFT_OWN_PRUNED:
         launches_per_step = 2 * len(c['Nd']) + 2
+    elif fkind.value == _lib.NUFFT_FFT_OWN_COILS:
+        # two coil-batched passes each way, k2y, y2k (deterministic: + the
+        # scale's two kernels and the rounding)
+        launches_per_step = 6 + (3 if args.deterministic else 0)
     else:
         launches_per_step = 4 if (c['batch'] or 1) == 1 else 6
 

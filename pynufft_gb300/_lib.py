@@ -26,7 +26,7 @@ NUFFT_ETIMEOUT = 9
 NUFFT_FLAG_DETERMINISTIC = 1
 NUFFT_FLAG_OWN_FFT = 2
 NUFFT_FLAG_CUFFT = 4
-NUFFT_FFT_CUFFT, NUFFT_FFT_CUFFT_PRUNED, NUFFT_FFT_OWN_PRUNED = 0, 1, 2
+NUFFT_FFT_CUFFT, NUFFT_FFT_CUFFT_PRUNED, NUFFT_FFT_OWN_PRUNED, NUFFT_FFT_OWN_COILS = 0, 1, 2, 3
 NUFFT_K2Y_ZTEAM, NUFFT_K2Y_POINT, NUFFT_K2Y_TILE, NUFFT_K2Y_TILE_POINT = 1, 2, 3, 4
 NUFFT_Y2K_ZTEAM, NUFFT_Y2K_POINT, NUFFT_Y2K_GLOBAL = 1, 2, 3
 

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, 'csrc')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libpynufft_gb300.so')
 SOURCES = ['capi.cu', 'plan_math.cpp', 'points.cu', 'interp.cu', 'interp_d1.cu', 'interp_d2.cu',
-           'interp_d3.cu', 'interp_cm2.cu', 'interp_cm3.cu', 'fftstage.cu', 'pfft.cu', 'cg.cu', 'tv.cu', 'noalloc.cu', 'selftest.cu']
+           'interp_d3.cu', 'interp_cm2.cu', 'interp_cm3.cu', 'fftstage.cu', 'pfft.cu', 'cfft.cu', 'cg.cu', 'tv.cu', 'noalloc.cu', 'selftest.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 

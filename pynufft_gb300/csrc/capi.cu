@@ -54,7 +54,7 @@ nufft::Geom nufft_plan_s::geom() const {
     g.rsub = d_rsub;
     g.nrsub = nrsub;
     g.rgroup = rgroup;
-    g.cm_il = cm_il ? 1 : 0;
+    g.cm_il = cfft ? 2 : (cm_il ? 1 : 0);
     // lane mappings: coil-teams for B >= 8; otherwise the plan's choice.  The
     // defaults (fastest in measurement on 2D radial and 3D uniform
     // trajectories; the autotuner may pick others): k2y gathers from a shared
@@ -302,8 +302,9 @@ int nufft_plan_transform_kind(nufft_plan_t p, int* kind) {
         set_error("nufft_plan_transform_kind: NULL argument");
         return NUFFT_EINVAL;
     }
-    *kind = p->pfft ? NUFFT_FFT_OWN_PRUNED
-                    : (p->fft_pruned ? NUFFT_FFT_CUFFT_PRUNED : NUFFT_FFT_CUFFT);
+    *kind = p->cfft ? NUFFT_FFT_OWN_COILS
+                    : p->pfft ? NUFFT_FFT_OWN_PRUNED
+                              : (p->fft_pruned ? NUFFT_FFT_CUFFT_PRUNED : NUFFT_FFT_CUFFT);
     return NUFFT_OK;
 }
 
@@ -452,6 +453,10 @@ int nufft_adjoint(nufft_plan_t p, const void* y, void* x, void* stream) {
         NUFFT_CUDA_TRY(cudaEventRecord(p->ev_adj, s));
         p->adj_used = true;
         return st;
+    }
+    if (cm_path(p) && p->cfft) {   // several coils, 2D: the coil-fastest grid, own passes
+        NUFFT_TRY(launch_y2k_cm(p, (const float2*)y, p->d_grid, s));
+        return cfft_inverse(p, p->d_grid, (float2*)x, true, false, s);
     }
     if (cm_path(p)) {   // several coils: the gridded spectra are written coil-major
         NUFFT_TRY(launch_y2k_cm(p, (const float2*)y, p->d_cm, s));

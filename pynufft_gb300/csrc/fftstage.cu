@@ -563,6 +563,7 @@ int cm_to_image(nufft_plan_s* p, float2* xx, bool apply_sn, bool divide_sn, cuda
 // transpose to coil-major, then cm_to_image.  k is read only.
 int image_from_spectrum_coils(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn,
                               bool divide_sn, cudaStream_t s) {
+    if (p->cfft) return cfft_inverse(p, k, xx, apply_sn, divide_sn, s);
     NUFFT_TRY(coil_transpose(p, k, p->d_cm, true, s));
     return cm_to_image(p, xx, apply_sn, divide_sn, s);
 }
@@ -643,6 +644,7 @@ int image_to_cm(nufft_plan_s* p, const float2* xx, bool apply_sn, cudaStream_t s
 // every call.
 int forward_from_image(nufft_plan_s* p, const float2* xx, bool apply_sn, float2* k,
                        cudaStream_t s, int dom_axis) {
+    if (p->cfft) return cfft_forward(p, xx, apply_sn, dom_axis, k, s);
     if (p->B > 1) {
         // coil-major: pad every coil's grid, transform there, transpose to k
         NUFFT_TRY(image_to_cm(p, xx, apply_sn, s, dom_axis));
@@ -677,10 +679,11 @@ int forward_from_image(nufft_plan_s* p, const float2* xx, bool apply_sn, float2*
     return NUFFT_OK;
 }
 
-// One coil: the own pruned passes, else the inverse cuFFT in place on k
-// followed by the crop.
+// The own coil-batched passes (2D, several coils), the own pruned passes
+// (one coil), else the inverse cuFFT in place on k followed by the crop.
 int image_from_spectrum(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn,
                         bool divide_sn, cudaStream_t s) {
+    if (p->cfft) return cfft_inverse(p, k, xx, apply_sn, divide_sn, s);
     if (p->pfft) return pfft_inverse(p, k, xx, apply_sn, divide_sn, s);
     float2* kk = const_cast<float2*>(k);
     NUFFT_TRY(fft_exec(p, kk, +1, s));
@@ -824,7 +827,8 @@ int fft_init(nufft_plan_s* p) {
     // (3D: only up to 1 GiB of spectra -- 8 coils at 192^3: pair 3.95 -> 3.74
     // ms; at 384^3, 3.6 GB, the per-system pruned plans below were 1.5%
     // faster: 31.1 against 31.5 ms)
-    p->cm_il = (B > 1 && p->ninst == 1 &&
+    p->cfft = cfft_eligible(p);
+    p->cm_il = (!p->cfft && B > 1 && p->ninst == 1 &&
                 (p->ndim == 2 ||
                  (p->ndim == 3 && sizeof(float2) * (size_t)B * p->prodK <= ((size_t)1 << 30))));
     if (p->cm_il) {
@@ -903,6 +907,7 @@ int fft_init(nufft_plan_s* p) {
         NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_rows, p->d_fftwork));
         NUFFT_CUFFT_TRY(cufftSetWorkArea(p->fft_cols, p->d_fftwork));
     }
+    NUFFT_TRY(cfft_init(p));
     // own pruned passes where the grid allows (they use d_padin / d_slabout
     // as their intermediate arrays)
     return pfft_init(p);
@@ -923,6 +928,7 @@ void fft_destroy(nufft_plan_s* p) {
     cudaFree(p->d_il_z);
     p->d_il_pad = p->d_il_z = nullptr;
     pfft_free(p);
+    cfft_free(p);
     cudaFree(p->d_fftwork);
     p->d_fftwork = nullptr;
     cudaFree(p->d_padin);

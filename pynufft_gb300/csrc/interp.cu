@@ -280,6 +280,9 @@ int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_
 // 8M-point kooshball: 19 ms against 111 ms for the coil-team kernel's
 // per-contribution 64-bit atomics); the others run launch_y2k.
 int launch_y2k_grid(nufft_plan_s* p, const float2* y, float2* k, cudaStream_t s) {
+    // plans with the coil-batched passes: the row kernels grid coil-fastest
+    // into k in either mode
+    if (p->cfft && cm_path(p)) return launch_y2k_cm(p, y, k, s);
     if ((p->flags & NUFFT_FLAG_DETERMINISTIC) && cm_path(p)) {
         NUFFT_TRY(launch_y2k_cm(p, y, p->d_cm, s));
         return cm_to_grid(p, k, s);
@@ -292,6 +295,7 @@ int launch_y2k_grid(nufft_plan_s* p, const float2* y, float2* k, cudaStream_t s)
 // Allocates nothing.
 int launch_y2k_exact_into(const nufft_plan_s* p, const float2* y, float2* grid,
                           unsigned long long* acc, double* scal, cudaStream_t s) {
+    if (cm_path(p) && p->cfft) return y2k_cm_det(p, y, grid, acc, scal, nullptr, s);
     if (cm_path(p)) {
         // plans with the row kernels: the deterministic stage's own path
         // (launch_y2k_grid), into the plan's coil-major buffer and one transpose

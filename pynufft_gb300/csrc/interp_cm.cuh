@@ -315,23 +315,36 @@ __global__ void __launch_bounds__(256, (DIM == 3) ? 3 : 0) y2k_rows_kernel(Geom 
                 // (X B + b) times the slab size)
                 const size_t X = interior ? o[0] + rx : wrapn(o[0] + rx, g.K[0]);
                 size_t rbase;
+                size_t cs = 1;   // element stride of consecutive cells of the row
                 if constexpr (DIM == 3) {
                     const size_t Y = interior ? o[1] + ry : wrapn(o[1] + ry, g.K[1]);
-                    rbase = g.cm_il ? ((X * B + b0 + b) * g.K[1] + Y) * Kz
-                                    : (ibase + b0 + b) * (size_t)g.prodK + (X * g.K[1] + Y) * Kz;
+                    if (g.cm_il == 2) {
+                        rbase = ((size_t)sp.w * g.prodK + (X * g.K[1] + Y) * Kz) * B + b0 + b;
+                        cs = B;
+                    } else {
+                        rbase = g.cm_il ? ((X * B + b0 + b) * g.K[1] + Y) * Kz
+                                        : (ibase + b0 + b) * (size_t)g.prodK + (X * g.K[1] + Y) * Kz;
+                    }
                 } else {
-                    rbase = g.cm_il ? (X * B + b0 + b) * Kz
-                                    : (ibase + b0 + b) * (size_t)g.prodK + X * Kz;
+                    if (g.cm_il == 2) {
+                        rbase = ((size_t)sp.w * g.prodK + X * Kz) * B + b0 + b;
+                        cs = B;
+                    } else {
+                        rbase = g.cm_il ? (X * B + b0 + b) * Kz
+                                        : (ibase + b0 + b) * (size_t)g.prodK + X * Kz;
+                    }
                 }
                 // a row holds TZ <= Kz cells, so it wraps at most once: cells
                 // [0, cw) from o_z on, cells [cw, TZ) from 0
                 const int cw = interior ? TZ : Kz - o[DI];
-                const size_t e0 = rbase + o[DI];
+                const size_t e0 = rbase + (size_t)o[DI] * cs;
 #pragma unroll
                 for (int c = 0; c < TZ; ++c) {
                     const float2 v = acc[c];
                     if (v.x == 0.f && v.y == 0.f) continue;
-                    const size_t e = e0 + ((c < cw) ? c : c - Kz);   // wrapped past the row end
+                    // (wrapped past the row end: back Kz cells)
+                    const size_t e =
+                        (size_t)((int64_t)e0 + (int64_t)((c < cw) ? c : c - Kz) * (int64_t)cs);
                     if constexpr (DET) {
                         atomicAdd(igrid + 2 * e, (unsigned long long)__float2ll_rn(v.x * fscale));
                         atomicAdd(igrid + 2 * e + 1, (unsigned long long)__float2ll_rn(v.y * fscale));

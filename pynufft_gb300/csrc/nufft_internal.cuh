@@ -89,7 +89,8 @@ struct Geom {
     const int4* rsub;            // row-gridding sub-problems (plans of 8+ coils):
     int64_t nrsub;               //   runs of <= kRowGroup bins along the innermost
     int rgroup;                  //   axis (rgroup bins), <= row_sub_cap points
-    int cm_il;                   // coil-major spectra row-interleaved (see nufft_plan_s)
+    int cm_il;                   // row gridding target: 0 coil-major, 1 coil-major
+                                 // row-interleaved (see nufft_plan_s), 2 coil-fastest
     int kmethod;                 // k2y lane mapping (NUFFT_K2Y_*), resolved
     int ymethod;                 // y2k lane mapping (NUFFT_Y2K_*), resolved
     int* kerr;                   // device flag: a bounded wait ran out (nufft_plan_check)
@@ -207,6 +208,12 @@ struct nufft_plan_s {
     bool pfft = false;                // own pruned power-of-two FFT passes (pfft.cu)
     float2* d_pfft_tw = nullptr;      // per-axis, per-stage twiddle tables, concatenated
     int pfft_tw_off[3][4] = {};       // [axis][stage] offsets into d_pfft_tw
+    // 2D plans of a multiple of 8 coils, one instance, Kd in {256, 384, 512,
+    // 640}: the own coil-batched passes (cfft.cu) transform the coil-fastest
+    // grid directly (d_cm holds their Nd[0] x Kd[1] x B intermediate), and
+    // the row gridding writes the coil-fastest grid
+    bool cfft = false;
+    float2* d_cfft_tw = nullptr;      // exp(-2 pi i m / Kd[0]), then / Kd[1]
     float2* d_cm = nullptr;           // B > 1: coil-major copy of the grid for the FFTs
     // B > 1 with per-system pruned 3D plans: zero-kept padded inputs (the
     // first Nd[0] slabs of every system) and slab-FFT outputs (slabs past
@@ -324,6 +331,15 @@ int pfft_init(nufft_plan_s* p);
 void pfft_free(nufft_plan_s* p);
 int pfft_forward(nufft_plan_s* p, const float2* x, bool apply_sn, float2* k, cudaStream_t s);
 int pfft_inverse(nufft_plan_s* p, const float2* k, float2* x, bool apply_sn, bool divide_sn,
+                 cudaStream_t s);
+
+// cfft.cu: own coil-batched passes on coil-fastest layouts (2D, several coils)
+bool cfft_eligible(const nufft_plan_s* p);
+int cfft_init(nufft_plan_s* p);
+void cfft_free(nufft_plan_s* p);
+int cfft_forward(nufft_plan_s* p, const float2* xx, bool apply_sn, int dom_axis, float2* k,
+                 cudaStream_t s);
+int cfft_inverse(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn, bool divide_sn,
                  cudaStream_t s);
 
 // cg.cu
