@@ -1,5 +1,5 @@
 // Coil-batched FFT passes on coil-fastest layouts: the image <-> spectrum
-// transforms of 2D plans of several coils (a multiple of 8) and one
+// transforms of 2D and 3D plans of several coils (a multiple of 8) and one
 // instance, with every Kd in {256, 384, 512, 640}.
 //
 // The reference's batch layout keeps the coil index fastest in the image,
@@ -19,6 +19,11 @@
 //            trajectory derivative)--> mid[n0][k1][b] --(columns)--> k[k0][k1][b]
 //   inverse  k[k0][k1][b] --(columns, k0 -> n0 < N0)--> mid[n0][k1][b]
 //            --(rows, k1 -> n1 < N1, x 1/prod(Kd), x sn or / sn)--> x[n0][n1][b]
+//
+// and in 3D the same with three passes (z on the image's rows, then y, then
+// x), each reading only the slabs the previous one left nonzero.  The
+// intermediate arrays live in the plan's coil-major buffer, which these
+// plans do not otherwise use.
 //
 // (the reference's xx2k / k2xx: zero-pad into the top-left corner and
 // numpy.fft.fftn / ifftn, nufft/_nufft_class_methods_cpu.py:232-249, 316-329).
@@ -43,11 +48,17 @@ struct CfftArgs {
     int nchunk;              // blocks per outer index: ceil(inner / kCW)
     int lin, lout;           // inputs read (the rest are zero), outputs written
     const float2* tw;        // exp(-2 pi i m / L), m < L
-    // image side: MODE 1 scales the input, MODE 2 the output (o = n0, l = n1)
-    const float* sn_o;
+    // image side (the pass along the last axis): MODE 1 scales the input,
+    // MODE 2 the output.  The outer index o is (oa, ob) = (o / nob, o % nob):
+    // n0 in 2D (nob = 1), (n0, n1) in 3D; l is the last axis's index.
+    const float* sn_a;
+    const float* sn_b;       // null in 2D
     const float* sn_l;
-    int apply_sn, divide_sn, dom_axis;
-    float half_o, half_l;    // N0 / 2, N1 / 2 (the trajectory derivative's centre)
+    int nob;
+    int apply_sn, divide_sn;
+    int dom;                 // -1, or the index the trajectory derivative multiplies by:
+                             // 0 oa, 1 ob, 2 l
+    float dom_half;          // N_a / 2 of that axis
     float norm;
 };
 
@@ -57,16 +68,25 @@ __device__ __forceinline__ float2 twiddle(const float2* tw, int m) {
     return INV ? make_float2(v.x, -v.y) : v;
 }
 
+__device__ __forceinline__ float sn_at(const CfftArgs& a, int o, int l) {
+    const int oa = o / a.nob, ob = o - oa * a.nob;
+    float v = __ldg(a.sn_a + oa) * __ldg(a.sn_l + l);
+    if (a.sn_b) v *= __ldg(a.sn_b + ob);
+    return v;
+}
+
 template <int MODE>
 __device__ __forceinline__ float2 pre_op(const CfftArgs& a, int o, int l, float2 v) {
     if constexpr (MODE == 1) {
         if (a.apply_sn) {
-            const float sc = __ldg(a.sn_o + o) * __ldg(a.sn_l + l);
+            const float sc = sn_at(a, o, l);
             v.x *= sc;
             v.y *= sc;
         }
-        if (a.dom_axis >= 0) {   // x -i (n_a - N_a / 2)
-            const float t = (a.dom_axis == 0) ? (float)o - a.half_o : (float)l - a.half_l;
+        if (a.dom >= 0) {   // x -i (n_a - N_a / 2)
+            const int oa = o / a.nob;
+            const int n = (a.dom == 0) ? oa : (a.dom == 1) ? o - oa * a.nob : l;
+            const float t = (float)n - a.dom_half;
             v = make_float2(t * v.y, -t * v.x);
         }
     }
@@ -76,7 +96,7 @@ __device__ __forceinline__ float2 pre_op(const CfftArgs& a, int o, int l, float2
 template <int MODE>
 __device__ __forceinline__ float2 post_op(const CfftArgs& a, int o, int l, float2 v) {
     if constexpr (MODE == 2) {
-        const float snv = __ldg(a.sn_o + o) * __ldg(a.sn_l + l);
+        const float snv = sn_at(a, o, l);
         float sc = a.norm;
         if (a.apply_sn) sc *= snv;
         v.x *= sc;
@@ -195,13 +215,35 @@ int run_len(int L, const CfftArgs& a, int64_t outer, cudaStream_t s) {
 
 bool length_ok(int L) { return L == 256 || L == 384 || L == 512 || L == 640; }
 
-CfftArgs image_args(const nufft_plan_s* p) {
+// the twiddle table of axis d
+const float2* axis_tw(const nufft_plan_s* p, int d) {
+    const float2* t = p->d_cfft_tw;
+    for (int e = 0; e < d; ++e) t += p->Kd[e];
+    return t;
+}
+
+// One pass along axis d of the coil-fastest array [outer][L][inner]:
+// in[o][l][e] (strides in_so, in_sl) -> out[o][l][e].  The pass along the
+// last axis carries the image side (sn, the trajectory derivative, the
+// normalisation).
+CfftArgs pass_args(const nufft_plan_s* p, const float2* in, float2* out, int d, int64_t in_so,
+                   int64_t out_so, int64_t inner, int lin, int lout) {
     CfftArgs a{};
-    a.sn_o = p->d_snd;
-    a.sn_l = p->d_snd + p->Nd[0];
-    a.half_o = 0.5f * (float)p->Nd[0];
-    a.half_l = 0.5f * (float)p->Nd[1];
-    a.dom_axis = -1;
+    a.in = in;
+    a.out = out;
+    a.in_so = in_so;
+    a.out_so = out_so;
+    a.in_sl = a.out_sl = inner;
+    a.inner = (int)inner;
+    a.nchunk = (int)((inner + kCW - 1) / kCW);
+    a.lin = lin;
+    a.lout = lout;
+    a.tw = axis_tw(p, d);
+    a.sn_a = p->d_snd;
+    a.sn_b = (p->ndim == 3) ? p->d_snd + p->Nd[0] : nullptr;
+    a.sn_l = p->d_snd + (p->ndim == 3 ? p->Nd[0] + p->Nd[1] : p->Nd[0]);
+    a.nob = (p->ndim == 3) ? p->Nd[1] : 1;
+    a.dom = -1;
     a.norm = 1.f;
     return a;
 }
@@ -210,23 +252,27 @@ CfftArgs image_args(const nufft_plan_s* p) {
 
 bool cfft_eligible(const nufft_plan_s* p) {
     if (p->flags & NUFFT_FLAG_CUFFT) return false;
-    if (p->ndim != 2 || p->ninst != 1 || p->B < 8 || p->B % kCW != 0) return false;
-    if (!length_ok(p->Kd[0]) || !length_ok(p->Kd[1])) return false;
-    // batch chunks of kCW columns over K1 B, and int32 indices in a pass
-    return (int64_t)p->Kd[0] * p->Kd[1] * p->B < ((int64_t)1 << 31);
+    if ((p->ndim != 2 && p->ndim != 3) || p->ninst != 1 || p->B < 8 || p->B % kCW != 0)
+        return false;
+    for (int d = 0; d < p->ndim; ++d)
+        if (!length_ok(p->Kd[d]) || p->Nd[d] > p->Kd[d]) return false;
+    // 3D: both intermediate arrays (N0 x K1 x K2 and N0 x N1 x K2, times B)
+    // fit in the coil-major buffer
+    if (p->ndim == 3 && (int64_t)p->Nd[0] * (p->Kd[1] + p->Nd[1]) > (int64_t)p->Kd[0] * p->Kd[1])
+        return false;
+    // 32-bit batch and block indices in a pass
+    return p->prodK * p->B < ((int64_t)1 << 31);
 }
 
 int cfft_init(nufft_plan_s* p) {
     if (!p->cfft) return NUFFT_OK;
-    // twiddle tables exp(-2 pi i m / L) for both axes' lengths, from double
-    const int L0 = p->Kd[0], L1 = p->Kd[1];
-    std::vector<float2> h((size_t)L0 + L1);
-    for (int d = 0; d < 2; ++d) {
+    // twiddle tables exp(-2 pi i m / L) for every axis's length, from double
+    std::vector<float2> h;
+    for (int d = 0; d < p->ndim; ++d) {
         const int L = p->Kd[d];
-        float2* t = h.data() + (d == 0 ? 0 : L0);
         for (int m = 0; m < L; ++m) {
             const double ang = -2.0 * M_PI * (double)m / (double)L;
-            t[m] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+            h.push_back(make_float2((float)std::cos(ang), (float)std::sin(ang)));
         }
     }
     NUFFT_CUDA_TRY(cudaMalloc(&p->d_cfft_tw, sizeof(float2) * h.size()));
@@ -242,76 +288,70 @@ void cfft_free(nufft_plan_s* p) {
     p->cfft = false;
 }
 
-// image xx (N0 x N1 x B) -> spectrum k (K0 x K1 x B), through p->d_cm
+// image xx (Nd x B) -> spectrum k (Kd x B), through p->d_cm; dom_axis >= 0
+// multiplies the image by -i (n_a - N_a/2) along that axis
 int cfft_forward(nufft_plan_s* p, const float2* xx, bool apply_sn, int dom_axis, float2* k,
                  cudaStream_t s) {
-    const int B = p->B, N0 = p->Nd[0], N1 = p->Nd[1], K0 = p->Kd[0], K1 = p->Kd[1];
-    float2* mid = p->d_cm;   // N0 x K1 x B
-    CfftArgs a = image_args(p);
-    // rows: x[n0][n1][b] -> mid[n0][k1][b]
-    a.in = xx;
-    a.out = mid;
-    a.in_so = (int64_t)N1 * B;
-    a.in_sl = B;
-    a.out_so = (int64_t)K1 * B;
-    a.out_sl = B;
-    a.inner = B;
-    a.nchunk = (B + kCW - 1) / kCW;
-    a.lin = N1;
-    a.lout = K1;
-    a.tw = p->d_cfft_tw + K0;
+    const int64_t B = p->B;
+    const int* N = p->Nd;
+    const int* K = p->Kd;
+    const int nd = p->ndim, last = nd - 1;
+    // the last axis: the image's rows -> mid (Nd[..last) x K[last] x B)
+    float2* mid = p->d_cm;
+    int64_t outer = 1;
+    for (int d = 0; d < last; ++d) outer *= N[d];
+    // 3D: mid2 (N0 x K1 x K2 x B) first in the buffer, mid1 (N0 x N1 x K2 x B) after it
+    float2* mid2 = p->d_cm;
+    float2* mid1 = (nd == 3) ? p->d_cm + (int64_t)N[0] * K[1] * K[2] * B : mid;
+    CfftArgs a = pass_args(p, xx, mid1, last, (int64_t)N[last] * B, (int64_t)K[last] * B, B,
+                           N[last], K[last]);
     a.apply_sn = apply_sn ? 1 : 0;
-    a.dom_axis = dom_axis;
-    NUFFT_TRY((run_len<false, 1>(K1, a, N0, s)));
-    // columns: mid[n0][k1 b] -> k[k0][k1 b]
-    CfftArgs c = image_args(p);
-    c.in = mid;
-    c.out = k;
-    c.in_so = c.out_so = 0;
-    c.in_sl = c.out_sl = (int64_t)K1 * B;
-    c.inner = K1 * B;
-    c.nchunk = (c.inner + kCW - 1) / kCW;
-    c.lin = N0;
-    c.lout = K0;
-    c.tw = p->d_cfft_tw;
-    return run_len<false, 0>(K0, c, 1, s);
+    if (dom_axis >= 0) {
+        a.dom = (dom_axis == last) ? 2 : dom_axis;
+        a.dom_half = 0.5f * (float)N[dom_axis];
+    }
+    NUFFT_TRY((run_len<false, 1>(K[last], a, outer, s)));
+    if (nd == 3) {   // y: mid1[n0][n1][k2 b] -> mid2[n0][k1][k2 b]
+        const int64_t in2 = (int64_t)K[2] * B;
+        CfftArgs c = pass_args(p, mid1, mid2, 1, (int64_t)N[1] * in2, (int64_t)K[1] * in2, in2,
+                               N[1], K[1]);
+        NUFFT_TRY((run_len<false, 0>(K[1], c, N[0], s)));
+    }
+    // x: [n0][rest] -> k[k0][rest]
+    const int64_t rest = p->prodK / K[0] * B;
+    CfftArgs c = pass_args(p, nd == 3 ? mid2 : mid1, k, 0, 0, 0, rest, N[0], K[0]);
+    return run_len<false, 0>(K[0], c, 1, s);
 }
 
-// spectrum k (K0 x K1 x B, read only) -> image xx (N0 x N1 x B): inverse
-// transform, crop, x 1/prod(Kd), x sn when apply_sn, / sn when divide_sn
+// spectrum k (Kd x B, read only) -> image xx (Nd x B): inverse transform,
+// crop, x 1/prod(Kd), x sn when apply_sn, / sn when divide_sn
 int cfft_inverse(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn, bool divide_sn,
                  cudaStream_t s) {
-    const int B = p->B, N0 = p->Nd[0], N1 = p->Nd[1], K0 = p->Kd[0], K1 = p->Kd[1];
-    float2* mid = p->d_cm;
-    // columns: k[k0][k1 b] -> mid[n0 < N0][k1 b]
-    CfftArgs c = image_args(p);
-    c.in = k;
-    c.out = mid;
-    c.in_so = c.out_so = 0;
-    c.in_sl = c.out_sl = (int64_t)K1 * B;
-    c.inner = K1 * B;
-    c.nchunk = (c.inner + kCW - 1) / kCW;
-    c.lin = K0;
-    c.lout = N0;
-    c.tw = p->d_cfft_tw;
-    NUFFT_TRY((run_len<true, 0>(K0, c, 1, s)));
-    // rows: mid[n0][k1][b] -> x[n0][n1 < N1][b]
-    CfftArgs a = image_args(p);
-    a.in = mid;
-    a.out = xx;
-    a.in_so = (int64_t)K1 * B;
-    a.in_sl = B;
-    a.out_so = (int64_t)N1 * B;
-    a.out_sl = B;
-    a.inner = B;
-    a.nchunk = (B + kCW - 1) / kCW;
-    a.lin = K1;
-    a.lout = N1;
-    a.tw = p->d_cfft_tw + K0;
+    const int64_t B = p->B;
+    const int* N = p->Nd;
+    const int* K = p->Kd;
+    const int nd = p->ndim, last = nd - 1;
+    float2* mid2 = p->d_cm;
+    float2* mid1 = (nd == 3) ? p->d_cm + (int64_t)N[0] * K[1] * K[2] * B : p->d_cm;
+    // x: k[k0][rest] -> [n0 < N0][rest]
+    const int64_t rest = p->prodK / K[0] * B;
+    CfftArgs c = pass_args(p, k, nd == 3 ? mid2 : mid1, 0, 0, 0, rest, K[0], N[0]);
+    NUFFT_TRY((run_len<true, 0>(K[0], c, 1, s)));
+    if (nd == 3) {   // y: mid2[n0][k1][k2 b] -> mid1[n0][n1 < N1][k2 b]
+        const int64_t in2 = (int64_t)K[2] * B;
+        CfftArgs c2 = pass_args(p, mid2, mid1, 1, (int64_t)K[1] * in2, (int64_t)N[1] * in2, in2,
+                                K[1], N[1]);
+        NUFFT_TRY((run_len<true, 0>(K[1], c2, N[0], s)));
+    }
+    // the last axis: mid1 -> the image's rows, cropped and scaled
+    int64_t outer = 1;
+    for (int d = 0; d < last; ++d) outer *= N[d];
+    CfftArgs a = pass_args(p, mid1, xx, last, (int64_t)K[last] * B, (int64_t)N[last] * B, B,
+                           K[last], N[last]);
     a.apply_sn = apply_sn ? 1 : 0;
     a.divide_sn = divide_sn ? 1 : 0;
     a.norm = (float)(1.0 / (double)p->prodK);
-    return run_len<true, 2>(K1, a, N0, s);
+    return run_len<true, 2>(K[last], a, outer, s);
 }
 
 }  // namespace nufft

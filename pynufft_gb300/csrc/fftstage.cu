@@ -856,7 +856,8 @@ int fft_init(nufft_plan_s* p) {
         NUFFT_TRY(make_plan(&p->fft_slab, p->ndim - 1, n + 1, 1, slab, p->Nd[0], &work));
         NUFFT_TRY(make_plan(&p->fft_x, 1, n, slab, 1, slab, &work));
         p->fft_pruned = true;
-    } else if (B > 1 && !p->cm_il && p->ndim == 3 && p->Nd[0] < p->Kd[0] && p->ninst * B <= 16) {
+    } else if (B > 1 && !p->cm_il && !p->cfft && p->ndim == 3 && p->Nd[0] < p->Kd[0] &&
+               p->ninst * B <= 16) {
         // coil-major spectra of a few 3D systems: the same pruned pair of
         // plans, run once per system
         const int slab = (int)(p->prodK / p->Kd[0]);

@@ -208,9 +208,9 @@ struct nufft_plan_s {
     bool pfft = false;                // own pruned power-of-two FFT passes (pfft.cu)
     float2* d_pfft_tw = nullptr;      // per-axis, per-stage twiddle tables, concatenated
     int pfft_tw_off[3][4] = {};       // [axis][stage] offsets into d_pfft_tw
-    // 2D plans of a multiple of 8 coils, one instance, Kd in {256, 384, 512,
-    // 640}: the own coil-batched passes (cfft.cu) transform the coil-fastest
-    // grid directly (d_cm holds their Nd[0] x Kd[1] x B intermediate), and
+    // 2D / 3D plans of a multiple of 8 coils, one instance, Kd in {256, 384,
+    // 512, 640}: the own coil-batched passes (cfft.cu) transform the
+    // coil-fastest grid directly (d_cm holds their intermediate arrays), and
     // the row gridding writes the coil-fastest grid
     bool cfft = false;
     float2* d_cfft_tw = nullptr;      // exp(-2 pi i m / Kd[0]), then / Kd[1]

@@ -1,9 +1,9 @@
-"""GPU parity of the own coil-batched FFT passes (NUFFT_FFT_OWN_COILS): 2D
+"""GPU parity of the own coil-batched FFT passes (NUFFT_FFT_OWN_COILS): 2D and 3D
 plans of a multiple of 8 coils and one instance with every Kd in
 {256, 384, 512, 640}.
 
 The passes transform the reference's batch layout, coil index fastest
-(linalg/nufft_hsa.py:203-228), in two pruned passes each way with the pad /
+(linalg/nufft_hsa.py:203-228), one pruned pass per axis each way with the pad /
 crop and the scaling fused (the reference's xx2k / k2xx: zero-pad into the
 top-left corner, numpy fftn / ifftn, nufft/_nufft_class_methods_cpu.py:232-249,
 316-329), and plans of a multiple of 32 coils grid straight into the
@@ -141,3 +141,52 @@ def test_coil_passes_cg_matches_cufft_plan(NUFFT):
     xa = A.solve(y, 'cg', maxiter=5)
     xc = C.solve(y, 'cg', maxiter=5)
     assert rel_l2(xa, xc) < 1e-4
+
+
+def test_coil_passes_3d_match_cufft_and_oracle(NUFFT):
+    """3D: three passes each way (z on the image's rows, then y, then x);
+    the 8-coil plan against the cuFFT plan on every stage, one coil against
+    the single-coil oracle, and the deterministic plan (row gridding into the
+    coil-fastest grid) bitwise on repeat."""
+    import torch
+    from pynufft_gb300 import _lib
+    rng = np.random.default_rng(21)
+    Nd, Kd, Jd, B = (100, 160, 128), (256, 384, 256), (6, 6, 6), 8
+    M = 20000
+    om = rng.uniform(-np.pi, np.pi, (M, 3))
+    A = NUFFT(0)
+    A.plan(om, Nd, Kd, Jd, batch=B)
+    assert kind(A) == _lib.NUFFT_FFT_OWN_COILS
+    C = NUFFT(0)
+    C.plan(om, Nd, Kd, Jd, batch=B, fft='cufft')
+    x = torch.from_numpy(cplx(rng, Nd + (B,))).cuda()
+    y = torch.from_numpy(cplx(rng, (M, B))).cuda()
+    k = torch.from_numpy(cplx(rng, Kd + (B,))).cuda()
+    for name, arg in [('xx2k', x), ('k2xx', k), ('forward', x), ('adjoint', y), ('y2k', y)]:
+        a = getattr(A, name)(arg)
+        c = getattr(C, name)(arg)
+        assert rel_l2(a.cpu().numpy(), c.cpu().numpy()) < TOL, name
+    O = OracleNUFFT()
+    O.plan(om, Nd, Kd, Jd)
+    b = 5
+    xb, kb, yb = (t.cpu().numpy()[..., b] for t in (x, k, y))
+    assert rel_l2(A.xx2k(x).cpu().numpy()[..., b], O.xx2k(xb)) < TOL
+    assert rel_l2(A.k2xx(k).cpu().numpy()[..., b], O.k2xx(kb)) < TOL
+    assert rel_l2(A.forward(x).cpu().numpy()[..., b], O.forward(xb)) < TOL
+    assert rel_l2(A.adjoint(y).cpu().numpy()[..., b], O.adjoint(yb)) < TOL
+
+    D = NUFFT(0)
+    D.plan(om, Nd, Kd, Jd, batch=B, deterministic=True)
+    assert kind(D) == _lib.NUFFT_FFT_OWN_COILS
+    x1, x2 = D.adjoint(y), D.adjoint(y)
+    assert torch.equal(x1, x2)
+    assert rel_l2(x1.cpu().numpy(), C.adjoint(y).cpu().numpy()) < TOL
+    outs = []
+    for P in (C, A):
+        dy = torch.empty((3, M, B), dtype=torch.complex64, device='cuda')
+        st = P._lib.nufft_forward_dom(P._plan, ctypes.c_void_p(x.data_ptr()),
+                                      ctypes.c_void_p(dy.data_ptr()),
+                                      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        assert st == _lib.NUFFT_OK
+        outs.append(dy.cpu().numpy())
+    assert rel_l2(outs[1], outs[0]) < TOL
