@@ -169,10 +169,10 @@ int nufft_plan_info(nufft_plan_t plan, int64_t* M_total, int64_t* n_subproblems,
  * NUFFT_FLAG_OWN_FFT set or -- without NUFFT_FLAG_CUFFT -- every Kd 256 and
  * every Nd 128 or 256, where the passes' specialised 256-point kernels beat
  * cuFFT), NUFFT_FFT_OWN_COILS (the library's coil-batched passes on the
- * coil-fastest layout, pruned and with the pad / crop / scaling fused: 2D,
- * a multiple of 8 coils, one instance, every Kd in {256, 384, 512, 640},
- * unless NUFFT_FLAG_CUFFT is set).  No counterpart in the reference (numpy
- * fftn / ifftn). */
+ * coil-fastest layout, pruned and with the pad / crop / scaling fused: 2D
+ * or 3D, a multiple of 8 coils, one instance, every Kd in {128, 160, 192,
+ * 256, 320, 384, 512, 640}, unless NUFFT_FLAG_CUFFT is set).  No
+ * counterpart in the reference (numpy fftn / ifftn). */
 #define NUFFT_FFT_CUFFT        0
 #define NUFFT_FFT_CUFFT_PRUNED 1
 #define NUFFT_FFT_OWN_PRUNED   2

@@ -1,6 +1,6 @@
 // Coil-batched FFT passes on coil-fastest layouts: the image <-> spectrum
 // transforms of 2D and 3D plans of several coils (a multiple of 8) and one
-// instance, with every Kd in {256, 384, 512, 640}.
+// instance, with every Kd in {128, 160, 192, 256, 320, 384, 512, 640}.
 //
 // The reference's batch layout keeps the coil index fastest in the image,
 // the spectrum and the samples (linalg/nufft_hsa.py:203-228).  These passes
@@ -9,7 +9,8 @@
 // strided axis whose batch (coils, or coils x cells) is contiguous.  A block
 // takes 8 contiguous batch elements (64 bytes per row) and runs their 8
 // transforms together: a mixed-radix Stockham FFT in three radix stages
-// (640 = 10 x 8 x 8, 512 = 8 x 8 x 8, 384 = 6 x 8 x 8, 256 = 4 x 8 x 8),
+// (640 = 10 x 8 x 8, 512 = 8 x 8 x 8, 384 = 6 x 8 x 8, 320 = 5 x 8 x 8,
+// 256 = 4 x 8 x 8, 192 = 6 x 4 x 8, 160 = 5 x 4 x 8, 128 = 2 x 8 x 8),
 // the first reading global memory, the last writing it, shared memory in
 // between, twiddles from a plan-time table.  Zero padding and cropping are
 // pruned (the first stage reads only the `lin` nonzero inputs, the last
@@ -206,14 +207,21 @@ int run_len(int L, const CfftArgs& a, int64_t outer, cudaStream_t s) {
         case 640: return run_pass<640, 10, 8, 8, INV, MODE>(a, outer, s);
         case 512: return run_pass<512, 8, 8, 8, INV, MODE>(a, outer, s);
         case 384: return run_pass<384, 6, 8, 8, INV, MODE>(a, outer, s);
+        case 320: return run_pass<320, 5, 8, 8, INV, MODE>(a, outer, s);
         case 256: return run_pass<256, 4, 8, 8, INV, MODE>(a, outer, s);
+        case 192: return run_pass<192, 6, 4, 8, INV, MODE>(a, outer, s);
+        case 160: return run_pass<160, 5, 4, 8, INV, MODE>(a, outer, s);
+        case 128: return run_pass<128, 2, 8, 8, INV, MODE>(a, outer, s);
         default:
             set_error("cfft: unsupported transform length");
             return NUFFT_EUNSUPPORTED;
     }
 }
 
-bool length_ok(int L) { return L == 256 || L == 384 || L == 512 || L == 640; }
+bool length_ok(int L) {
+    return L == 128 || L == 160 || L == 192 || L == 256 || L == 320 || L == 384 || L == 512 ||
+           L == 640;
+}
 
 // the twiddle table of axis d
 const float2* axis_tw(const nufft_plan_s* p, int d) {

@@ -208,8 +208,8 @@ struct nufft_plan_s {
     bool pfft = false;                // own pruned power-of-two FFT passes (pfft.cu)
     float2* d_pfft_tw = nullptr;      // per-axis, per-stage twiddle tables, concatenated
     int pfft_tw_off[3][4] = {};       // [axis][stage] offsets into d_pfft_tw
-    // 2D / 3D plans of a multiple of 8 coils, one instance, Kd in {256, 384,
-    // 512, 640}: the own coil-batched passes (cfft.cu) transform the
+    // 2D / 3D plans of a multiple of 8 coils, one instance, Kd in {128, 160,
+    // 192, 256, 320, 384, 512, 640}: the own coil-batched passes (cfft.cu) transform the
     // coil-fastest grid directly (d_cm holds their intermediate arrays), and
     // the row gridding writes the coil-fastest grid
     bool cfft = false;
