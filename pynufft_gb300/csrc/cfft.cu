@@ -40,13 +40,15 @@ namespace {
 using cdft::kCW;
 using cdft::Plan3;
 
+// Element offsets fit 32 bits (the plans these passes serve hold fewer than
+// 2^31 grid elements), and the batch is a multiple of kCW.
 struct CfftArgs {
     const float2* in;
     float2* out;
-    int64_t in_so, in_sl;    // input strides (elements) of the outer and transform indices
-    int64_t out_so, out_sl;  // output strides
+    int in_so, in_sl;        // input strides (elements) of the outer and transform indices
+    int out_so, out_sl;      // output strides
     int inner;               // batch elements per (outer, index)
-    int nchunk;              // blocks per outer index: ceil(inner / kCW)
+    int nchunk;              // blocks per outer index: inner / kCW
     int lin, lout;           // inputs read (the rest are zero), outputs written
     const float2* tw;        // exp(-2 pi i m / L), m < L
     // image side (the pass along the last axis): MODE 1 scales the input,
@@ -144,25 +146,21 @@ __global__ void __launch_bounds__(Plan3<L, R0, R1, R2>::THREADS)
     const int w = threadIdx.x % kCW, j = threadIdx.x / kCW;
     const int o = blockIdx.x / a.nchunk, ch = blockIdx.x - o * a.nchunk;
     const int e = ch * kCW + w;   // batch element
-    const bool ok = e < a.inner;
-    const float2* __restrict__ in = a.in + o * a.in_so + e;
-    float2* __restrict__ out = a.out + o * a.out_so + e;
+    const float2* __restrict__ in = a.in + (o * a.in_so + e);
+    float2* __restrict__ out = a.out + (o * a.out_so + e);
 
-    {   // stage 0: global -> shared (inputs past lin are zero)
+    {   // stage 0: global -> shared (inputs past lin are zero); the barrier
+        // after it also publishes the twiddle table
         using S = typename P::S0;
-        float2 v[R0];
-        const bool act = j < S::NB;
-        if (act) {
+        if (j < S::NB) {
+            float2 v[R0];
 #pragma unroll
             for (int r = 0; r < R0; ++r) {
                 const int l = S::in_index(j, r);
-                v[r] = (ok && l < a.lin) ? pre_op<MODE>(a, o, l, __ldg(in + l * a.in_sl))
-                                         : make_float2(0.f, 0.f);
+                v[r] = (l < a.lin) ? pre_op<MODE>(a, o, l, __ldg(in + l * a.in_sl))
+                                   : make_float2(0.f, 0.f);
             }
             cdft::dft<R0, INV>(v);
-        }
-        __syncthreads();   // the twiddle table is in place
-        if (act) {
 #pragma unroll
             for (int r = 0; r < R0; ++r) buf[P::row(S::out_index(j, r)) * kCW + w] = v[r];
         }
@@ -179,12 +177,10 @@ __global__ void __launch_bounds__(Plan3<L, R0, R1, R2>::THREADS)
                 if (r > 0) v[r] = cdft::mul(v[r], twiddle<INV>(tw, S::tw_index(j, r)));
             }
             cdft::dft<R2, INV>(v);
-            if (ok) {
 #pragma unroll
-                for (int r = 0; r < R2; ++r) {
-                    const int l = S::out_index(j, r);
-                    if (l < a.lout) out[l * a.out_sl] = post_op<MODE>(a, o, l, v[r]);
-                }
+            for (int r = 0; r < R2; ++r) {
+                const int l = S::out_index(j, r);
+                if (l < a.lout) out[l * a.out_sl] = post_op<MODE>(a, o, l, v[r]);
             }
         }
     }
@@ -197,6 +193,10 @@ int run_pass(const CfftArgs& a, int64_t outer, cudaStream_t s) {
     NUFFT_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)P::SMEM));
     const int64_t blocks = outer * a.nchunk;
+    if (a.inner % kCW != 0 || blocks >= ((int64_t)1 << 31)) {
+        set_error("cfft: batch not a multiple of 8 or too many blocks");
+        return NUFFT_EUNSUPPORTED;
+    }
     if (blocks > 0) kern<<<(unsigned)blocks, P::THREADS, P::SMEM, s>>>(a);
     return check_launch("cfft_pass_kernel");
 }
@@ -239,11 +239,11 @@ CfftArgs pass_args(const nufft_plan_s* p, const float2* in, float2* out, int d, 
     CfftArgs a{};
     a.in = in;
     a.out = out;
-    a.in_so = in_so;
-    a.out_so = out_so;
-    a.in_sl = a.out_sl = inner;
+    a.in_so = (int)in_so;
+    a.out_so = (int)out_so;
+    a.in_sl = a.out_sl = (int)inner;
     a.inner = (int)inner;
-    a.nchunk = (int)((inner + kCW - 1) / kCW);
+    a.nchunk = (int)(inner / kCW);
     a.lin = lin;
     a.lout = lout;
     a.tw = axis_tw(p, d);
