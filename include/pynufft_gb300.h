@@ -255,7 +255,8 @@ int nufft_adjoint_many2one(nufft_plan_t plan, const void* y, void* x, void* stre
  * every contribution summed exactly, or, on plans of 8 or more coils that
  * grid by tile rows, per-row float sums in a fixed order combined exactly
  * (those plans also use their coil-major spectrum buffer, allocated with the
- * plan, before one transpose into k). */
+ * plan, before one transpose into k, unless they run the coil-batched FFT
+ * passes: then the rows go straight into k). */
 #define NUFFT_STATIC_SCRATCH_CELLS (1u << 20)
 int nufft_y2k_exact_static(nufft_plan_t plan, const void* y, void* k, void* stream);
 

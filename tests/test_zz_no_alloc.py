@@ -33,6 +33,11 @@ def _cplx(rng, shape):
 
 
 def _geometry(case):
+    if case == 'coil_passes':
+        # 2D, a multiple of 32 coils, Kd 128: plans with the coil-batched FFT
+        # passes, whose row gridding writes the coil-fastest grid directly
+        rng = np.random.default_rng(17)
+        return [rng.uniform(-np.pi, np.pi, (4000, 2))], (64, 64), (128, 128), (6, 6)
     if case == 'instances':
         rng = np.random.default_rng(71)
         oms = [rng.uniform(-np.pi, np.pi, (m, 2)) for m in (900, 1, 2500, 300)]
@@ -54,7 +59,8 @@ def _plan(NUFFT, oms, Nd, Kd, Jd, batch, det):
 @pytest.mark.parametrize('case,batch,det', [('plan_2d', None, True), ('plan_3d', None, True),
                                             ('plan_2d', 3, True), ('plan_2d', None, False),
                                             ('plan_3d', 8, False), ('plan_2d', 32, False),
-                                            ('instances', None, False), ('instances', 2, True)])
+                                            ('instances', None, False), ('instances', 2, True),
+                                            ('coil_passes', 32, False), ('coil_passes', 32, True)])
 def test_no_alloc_gridding_matches_existing_entry_point(case, batch, det):
     import torch
     from pynufft_gb300 import NUFFT, _lib
