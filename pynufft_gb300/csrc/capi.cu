@@ -180,7 +180,9 @@ int nufft_plan_create(int ndim, const int* Nd, const int* Kd, const int* Jd, int
         return fail(e == cudaErrorMemoryAllocation ? NUFFT_ENOMEM : NUFFT_ECUDA);
     }
     p->dev_bytes = sizeof(float) * sumN + sizeof(AxisConst) * 3 + sizeof(float2) * ncell;
-    if (batch == 1 && ninst == 1 && !(flags & NUFFT_FLAG_DETERMINISTIC)) {
+    // fast mode, one coil or the coil-batched FFT passes: a second grid for
+    // the adjoint, zeroed on a side stream while the forward runs
+    if (!(flags & NUFFT_FLAG_DETERMINISTIC) && ((batch == 1 && ninst == 1) || cfft_eligible(p))) {
         e = cudaMalloc(&p->d_grid_adj, sizeof(float2) * ncell);
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->zs, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_zero, cudaEventDisableTiming);
@@ -429,7 +431,8 @@ int nufft_forward(nufft_plan_t p, const void* x, void* y, void* stream) {
         // zero the adjoint's grid on the side stream, after the last adjoint
         // has read it, while this forward runs
         if (p->adj_used) NUFFT_CUDA_TRY(cudaStreamWaitEvent(p->zs, p->ev_adj, 0));
-        NUFFT_CUDA_TRY(cudaMemsetAsync(p->d_grid_adj, 0, sizeof(float2) * p->prodK, p->zs));
+        NUFFT_CUDA_TRY(cudaMemsetAsync(p->d_grid_adj, 0,
+                                       sizeof(float2) * p->prodK * p->B * p->ninst, p->zs));
         NUFFT_CUDA_TRY(cudaEventRecord(p->ev_zero, p->zs));
         p->adj_zeroed = true;
     }
@@ -448,7 +451,10 @@ int nufft_adjoint(nufft_plan_t p, const void* y, void* x, void* stream) {
             pre = true;
         }
         p->adj_zeroed = false;   // consumed (or zeroed inline below)
-        NUFFT_TRY(launch_y2k(p, (const float2*)y, p->d_grid_adj, s, pre));
+        if (cm_path(p))   // several coils: the row gridding, coil-fastest
+            NUFFT_TRY(launch_y2k_cm(p, (const float2*)y, p->d_grid_adj, s, pre));
+        else
+            NUFFT_TRY(launch_y2k(p, (const float2*)y, p->d_grid_adj, s, pre));
         const int st = image_from_spectrum(p, p->d_grid_adj, (float2*)x, true, false, s);
         NUFFT_CUDA_TRY(cudaEventRecord(p->ev_adj, s));
         p->adj_used = true;

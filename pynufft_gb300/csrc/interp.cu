@@ -251,12 +251,13 @@ static int y2k_cm_det(const nufft_plan_s* p, const float2* y, float2* grid_cm,
     return check_launch("fixed_to_float_kernel");
 }
 
-int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s) {
+int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s,
+                  bool pre_zeroed) {
     const size_t ncells = (size_t)p->ninst * p->prodK * p->B;
     if (!(p->flags & NUFFT_FLAG_DETERMINISTIC)) {
         Geom g = p->geom();
         const int jm = pick_jm(p);
-        NUFFT_CUDA_TRY(cudaMemsetAsync(grid_cm, 0, sizeof(float2) * ncells, s));
+        if (!pre_zeroed) NUFFT_CUDA_TRY(cudaMemsetAsync(grid_cm, 0, sizeof(float2) * ncells, s));
         if (p->M == 0) return NUFFT_OK;
         const bool timed = kernel_time_start(p, 1, s);
         const int st = (p->ndim == 2) ? y2k_cm_dim2(jm, false, g, y, grid_cm, nullptr, nullptr, s)

@@ -293,7 +293,8 @@ int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s,
 // coil-major gridding (plans of 8 or more coils, interp_cm.cuh): whether the
 // plan's geometry has the row kernels, and y2k into the p->d_cm layout
 bool cm_path(const nufft_plan_s* p);
-int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s);
+int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s,
+                  bool pre_zeroed = false);
 // the y2k stage into a coil-fastest spectrum (the row kernels and one
 // transpose for deterministic plans that have them, else launch_y2k)
 int launch_y2k_grid(nufft_plan_s* p, const float2* y, float2* k, cudaStream_t s);
