@@ -550,9 +550,9 @@ def main():
     if fkind.value == _lib.NUFFT_FFT_OWN_PRUNED:
         launches_per_step = 2 * len(c['Nd']) + 2
     elif fkind.value == _lib.NUFFT_FFT_OWN_COILS:
-        # two coil-batched passes each way, k2y, y2k (deterministic: + the
-        # scale's two kernels and the rounding)
-        launches_per_step = 6 + (3 if args.deterministic else 0)
+        # the coil-batched passes (2 or 3 each way), k2y, y2k (deterministic:
+        # + the scale's two kernels; the first inverse pass rounds the sums)
+        launches_per_step = 2 * len(c['Nd']) + 2 + (2 if args.deterministic else 0)
     else:
         launches_per_step = 4 if (c['batch'] or 1) == 1 else 6
 

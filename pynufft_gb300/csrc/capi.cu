@@ -460,7 +460,13 @@ int nufft_adjoint(nufft_plan_t p, const void* y, void* x, void* stream) {
         p->adj_used = true;
         return st;
     }
-    if (cm_path(p) && p->cfft) {   // several coils, 2D: the coil-fastest grid, own passes
+    if (cm_path(p) && p->cfft) {   // several coils: the coil-fastest grid, own passes
+        if (p->flags & NUFFT_FLAG_DETERMINISTIC) {
+            // the exact sums rounded by the first inverse pass as it reads
+            // them (no separate rounding pass over the grid)
+            NUFFT_TRY(launch_y2k_cm_fixed(p, (const float2*)y, s));
+            return cfft_inverse_fixed(p, p->d_igrid, p->d_dscal, (float2*)x, true, false, s);
+        }
         NUFFT_TRY(launch_y2k_cm(p, (const float2*)y, p->d_grid, s));
         return cfft_inverse(p, p->d_grid, (float2*)x, true, false, s);
     }

@@ -63,6 +63,10 @@ struct CfftArgs {
                              // 0 oa, 1 ob, 2 l
     float dom_half;          // N_a / 2 of that axis
     float norm;
+    // MODE 3 (the first inverse pass of a deterministic adjoint): `in` holds
+    // the 64-bit fixed-point sums (re, im per element) that dscal[1] scales,
+    // rounded here as the separate rounding kernel would
+    const double* dscal;
 };
 
 template <bool INV>
@@ -148,6 +152,11 @@ __global__ void __launch_bounds__(Plan3<L, R0, R1, R2>::THREADS)
     const int e = ch * kCW + w;   // batch element
     const float2* __restrict__ in = a.in + (o * a.in_so + e);
     float2* __restrict__ out = a.out + (o * a.out_so + e);
+    // MODE 3: (re, im) fixed-point pairs, 16 bytes per element
+    const ulonglong2* __restrict__ fin =
+        reinterpret_cast<const ulonglong2*>(a.in) + (o * a.in_so + e);
+    float finv = 1.f;
+    if constexpr (MODE == 3) finv = (float)(1.0 / __ldg(a.dscal + 1));
 
     {   // stage 0: global -> shared (inputs past lin are zero); the barrier
         // after it also publishes the twiddle table
@@ -157,8 +166,18 @@ __global__ void __launch_bounds__(Plan3<L, R0, R1, R2>::THREADS)
 #pragma unroll
             for (int r = 0; r < R0; ++r) {
                 const int l = S::in_index(j, r);
-                v[r] = (l < a.lin) ? pre_op<MODE>(a, o, l, __ldg(in + l * a.in_sl))
-                                   : make_float2(0.f, 0.f);
+                if constexpr (MODE == 3) {
+                    if (l < a.lin) {
+                        const ulonglong2 q = __ldg(fin + l * a.in_sl);
+                        v[r] = make_float2(__ll2float_rn((long long)q.x) * finv,
+                                           __ll2float_rn((long long)q.y) * finv);
+                    } else {
+                        v[r] = make_float2(0.f, 0.f);
+                    }
+                } else {
+                    v[r] = (l < a.lin) ? pre_op<MODE>(a, o, l, __ldg(in + l * a.in_sl))
+                                       : make_float2(0.f, 0.f);
+                }
             }
             cdft::dft<R0, INV>(v);
 #pragma unroll
@@ -332,9 +351,11 @@ int cfft_forward(nufft_plan_s* p, const float2* xx, bool apply_sn, int dom_axis,
 }
 
 // spectrum k (Kd x B, read only) -> image xx (Nd x B): inverse transform,
-// crop, x 1/prod(Kd), x sn when apply_sn, / sn when divide_sn
-int cfft_inverse(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn, bool divide_sn,
-                 cudaStream_t s) {
+// crop, x 1/prod(Kd), x sn when apply_sn, / sn when divide_sn.  With
+// dscal, k is the 64-bit fixed-point sums of a deterministic gridding
+// (2 x Kd x B, re and im), rounded by the first pass.
+static int cfft_inverse_any(nufft_plan_s* p, const float2* k, const double* dscal, float2* xx,
+                            bool apply_sn, bool divide_sn, cudaStream_t s) {
     const int64_t B = p->B;
     const int* N = p->Nd;
     const int* K = p->Kd;
@@ -344,7 +365,11 @@ int cfft_inverse(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn, bo
     // x: k[k0][rest] -> [n0 < N0][rest]
     const int64_t rest = p->prodK / K[0] * B;
     CfftArgs c = pass_args(p, k, nd == 3 ? mid2 : mid1, 0, 0, 0, rest, K[0], N[0]);
-    NUFFT_TRY((run_len<true, 0>(K[0], c, 1, s)));
+    c.dscal = dscal;
+    if (dscal)
+        NUFFT_TRY((run_len<true, 3>(K[0], c, 1, s)));
+    else
+        NUFFT_TRY((run_len<true, 0>(K[0], c, 1, s)));
     if (nd == 3) {   // y: mid2[n0][k1][k2 b] -> mid1[n0][n1 < N1][k2 b]
         const int64_t in2 = (int64_t)K[2] * B;
         CfftArgs c2 = pass_args(p, mid2, mid1, 1, (int64_t)K[1] * in2, (int64_t)N[1] * in2, in2,
@@ -360,6 +385,17 @@ int cfft_inverse(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn, bo
     a.divide_sn = divide_sn ? 1 : 0;
     a.norm = (float)(1.0 / (double)p->prodK);
     return run_len<true, 2>(K[last], a, outer, s);
+}
+
+int cfft_inverse(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn, bool divide_sn,
+                 cudaStream_t s) {
+    return cfft_inverse_any(p, k, nullptr, xx, apply_sn, divide_sn, s);
+}
+
+int cfft_inverse_fixed(nufft_plan_s* p, const unsigned long long* ig, const double* dscal,
+                       float2* xx, bool apply_sn, bool divide_sn, cudaStream_t s) {
+    return cfft_inverse_any(p, reinterpret_cast<const float2*>(ig), dscal, xx, apply_sn, divide_sn,
+                            s);
 }
 
 }  // namespace nufft

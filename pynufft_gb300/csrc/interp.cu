@@ -225,7 +225,8 @@ bool cm_path(const nufft_plan_s* p) {
 // float sums in a fixed order, combined across tiles exactly in 64-bit fixed
 // point (igrid: 2 * ninst * prodK * B accumulators), then one rounding to
 // float; dscal holds kScaleSlots doubles.  Allocates nothing.  `timer`: the
-// plan whose kernel timing covers the launch, or null.
+// plan whose kernel timing covers the launch, or null.  grid_cm null: the
+// sums stay unrounded in igrid (for the coil-batched inverse passes).
 static int y2k_cm_det(const nufft_plan_s* p, const float2* y, float2* grid_cm,
                       unsigned long long* igrid, double* dscal, nufft_plan_s* timer,
                       cudaStream_t s) {
@@ -245,10 +246,31 @@ static int y2k_cm_det(const nufft_plan_s* p, const float2* y, float2* grid_cm,
         if (timer) kernel_time_stop(timer, 1, s, timed);
         NUFFT_TRY(st);
     }
+    if (!grid_cm) return NUFFT_OK;
     const int blocks = (int)std::min<size_t>((ncells + 255) / 256, (size_t)p->num_sms * 16);
     fixed_to_float_kernel<<<std::max(blocks, 1), 256, 0, s>>>(igrid, (int64_t)ncells, dscal,
                                                                grid_cm);
     return check_launch("fixed_to_float_kernel");
+}
+
+static int ensure_fixed_buffers(nufft_plan_s* p) {
+    const size_t ncells = (size_t)p->ninst * p->prodK * p->B;
+    if (!p->d_igrid) {
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_igrid, sizeof(unsigned long long) * 2 * ncells));
+        p->dev_bytes += sizeof(unsigned long long) * 2 * ncells;
+    }
+    if (!p->d_dscal) {
+        NUFFT_CUDA_TRY(cudaMalloc(&p->d_dscal, sizeof(double) * kScaleSlots));
+        p->dev_bytes += sizeof(double) * kScaleSlots;
+    }
+    return NUFFT_OK;
+}
+
+// Deterministic row gridding whose exact sums stay in p->d_igrid (scale in
+// p->d_dscal), for the coil-batched inverse passes to round as they read.
+int launch_y2k_cm_fixed(nufft_plan_s* p, const float2* y, cudaStream_t s) {
+    NUFFT_TRY(ensure_fixed_buffers(p));
+    return y2k_cm_det(p, y, nullptr, p->d_igrid, p->d_dscal, p, s);
 }
 
 int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s,
@@ -265,14 +287,7 @@ int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_
         kernel_time_stop(p, 1, s, timed);
         return st;
     }
-    if (!p->d_igrid) {
-        NUFFT_CUDA_TRY(cudaMalloc(&p->d_igrid, sizeof(unsigned long long) * 2 * ncells));
-        p->dev_bytes += sizeof(unsigned long long) * 2 * ncells;
-    }
-    if (!p->d_dscal) {
-        NUFFT_CUDA_TRY(cudaMalloc(&p->d_dscal, sizeof(double) * kScaleSlots));
-        p->dev_bytes += sizeof(double) * kScaleSlots;
-    }
+    NUFFT_TRY(ensure_fixed_buffers(p));
     return y2k_cm_det(p, y, grid_cm, p->d_igrid, p->d_dscal, p, s);
 }
 

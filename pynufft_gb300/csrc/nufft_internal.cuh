@@ -295,6 +295,9 @@ int launch_y2k(nufft_plan_s* p, const float2* y, float2* grid, cudaStream_t s,
 bool cm_path(const nufft_plan_s* p);
 int launch_y2k_cm(nufft_plan_s* p, const float2* y, float2* grid_cm, cudaStream_t s,
                   bool pre_zeroed = false);
+// deterministic plans: the row gridding's exact sums left in p->d_igrid
+// (scale in p->d_dscal), unrounded
+int launch_y2k_cm_fixed(nufft_plan_s* p, const float2* y, cudaStream_t s);
 // the y2k stage into a coil-fastest spectrum (the row kernels and one
 // transpose for deterministic plans that have them, else launch_y2k)
 int launch_y2k_grid(nufft_plan_s* p, const float2* y, float2* k, cudaStream_t s);
@@ -342,6 +345,10 @@ int cfft_forward(nufft_plan_s* p, const float2* xx, bool apply_sn, int dom_axis,
                  cudaStream_t s);
 int cfft_inverse(nufft_plan_s* p, const float2* k, float2* xx, bool apply_sn, bool divide_sn,
                  cudaStream_t s);
+// the same from a deterministic gridding's 64-bit fixed-point sums (ig: 2 x
+// prod(Kd) x B; dscal[1] their scale), rounded inside the first pass
+int cfft_inverse_fixed(nufft_plan_s* p, const unsigned long long* ig, const double* dscal,
+                       float2* xx, bool apply_sn, bool divide_sn, cudaStream_t s);
 
 // cg.cu
 int solve_cg(nufft_plan_s* p, const float2* y, float2* x, int maxiter, double rtol,
