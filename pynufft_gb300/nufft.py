@@ -77,12 +77,14 @@ class NUFFT:
         gridding mode.  ``bins``/``max_sub_points`` override the gridding bin
         shape; ``autotune=True`` applies the cached best setting for this
         geometry and point density, or searches once (``pynufft_gb300.autotune``).
-        ``fft`` picks the image <-> spectrum transform: ``'own'`` the
-        library's own pruned power-of-two passes where the plan allows them
-        (one coil, 2D/3D, every Kd a power of two), ``'cufft'`` cuFFT, and the
-        default ``'auto'`` the own passes where their specialised 256-point
-        kernels apply (every Kd 256, every Nd 128 or 256: faster than cuFFT
-        on a GB300) and cuFFT elsewhere.  Returns 0.
+        ``fft`` picks the image <-> spectrum transform: ``'cufft'`` cuFFT
+        everywhere; ``'auto'`` (the default) the library's own passes where
+        they are faster than cuFFT on a GB300 -- one coil with every Kd 256
+        and every Nd 128 or 256, and a multiple of 8 coils (one instance,
+        2D/3D) with every Kd in {128, 160, 192, 256, 320, 384, 512, 640}, the
+        coil-batched passes on the coil-fastest layout -- and cuFFT
+        elsewhere; ``'own'`` as ``'auto'``, plus the own pruned power-of-two
+        passes on any one-coil 2D/3D plan whose Kd are powers of two.  Returns 0.
         """
         self._check_shapes(Nd, Kd, Jd)
         if fft not in ('auto', 'cufft', 'own'):
