@@ -1,9 +1,9 @@
 """GPU parity: the CUDA path (through the C ABI) against the reference's own
 outputs (golden fixtures), the oracle, and the exact NDFT.
 
-Tolerance: the spec bar is 1e-5 relative L2 against the reference's
-numpy NUFFT on the same inputs; float32 gridding/FFT typically lands at
-1e-7..1e-6.  Every test states the bound it asserts.
+Tolerance: 1e-5 relative L2 against the reference's numpy NUFFT on the same
+inputs; float32 gridding/FFT typically lands at 1e-7..1e-6.  Every test
+states the bound it asserts.
 """
 import numpy as np
 import pytest
